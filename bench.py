@@ -1,0 +1,409 @@
+"""Benchmark: DIRBE 25 um line-of-sight throughput on GB300 (one JSON line).
+
+Workload (one step): the DIRBE model (Kelsall-98, 6 components) at 25 um over
+the full HEALPix nside-512 sky (3,145,728 pixel-centre directions, ecliptic),
+observer at (0.7071, 0.7071, 0) AU, Gauss-Legendre degree 50, float32-bulk
+kernel, per-component + total outputs.  Inputs are synthetic (HEALPix centres
+computed here); no dataset is involved.
+
+  value     LOS/s of the float32 kernel with inputs resident in HBM
+  e2e       LOS/s through Model.evaluate_xyz from pinned host memory (H2D of
+            the unit vectors and D2H of the total map inside the timed region)
+  extras    float64 plain-kernel LOS/s, float32-vs-float64 max/median relative
+            error over the full map, XU roofline fraction, CPU baseline
+
+`--impl reference` times the CPU restatement of ZodiPy's numpy path (the
+oracle, split over all host cores with a fork pool exactly like the
+reference's `nprocesses`) on a bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "LOS/s DIRBE 25µm nside512: FP32 vs FP64 GPU at ≤1e-5 rel err; fwd+bwd ms"
+NSIDE = 512
+OBSPOS = np.array([0.7071, 0.7071, 0.0])
+OBSTIME = "2022-01-01T00:00:00"
+CPU_SAMPLE = 1 << 18
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nside", type=int, default=NSIDE)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def build_model(precision="float32"):
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import units as u
+
+    return zg.Model(25 * u.micron, name="dirbe", gauss_quad_degree=50, precision=precision)
+
+
+def oracle_desc(model):
+    from zodipy_gb300.zodiacal_light_model import COMPONENT_CUTOFFS
+
+    m = model.get_parameters()
+    sp = model._spectrum
+    return {
+        "labels": list(m["comps"]),
+        "comps": m["comps"],
+        "cutoffs": {lbl.value: COMPONENT_CUTOFFS[lbl] for lbl in model._ipd_model.comps},
+        "T_0": m["T_0"],
+        "delta": m["delta"],
+        "emissivity": sp["emissivity"],
+        "albedo": sp["albedo"],
+        "C1": sp["C1"],
+        "C2": sp["C2"],
+        "C3": sp["C3"],
+        "solar_irradiance": sp["solar_irradiance"],
+        "bb_table": model._b_nu_table,
+        "gauss_quad_degree": 50,
+    }
+
+
+def workload(nside, rank=0, world=1):
+    from zodipy_gb300.ephemeris import earth_position, iso_to_mjd
+    from zodipy_gb300.healpix import pix2vec_ring
+
+    u = pix2vec_ring(nside)
+    ang = 2 * np.pi * rank / max(world, 1)  # weak scaling: each rank its own observer
+    rot = np.array([[np.cos(ang), -np.sin(ang), 0.0], [np.sin(ang), np.cos(ang), 0.0], [0.0, 0.0, 1.0]])
+    return u, rot @ OBSPOS, earth_position(iso_to_mjd(OBSTIME))
+
+
+def cpu_sample_run(nside, n_sample, reps):
+    """Time the oracle (ZodiPy's numpy path) over all host cores; returns (LOS/s, cores, secs)."""
+    from oracle import zodi_oracle as zo
+
+    model = build_model("float64")
+    desc = oracle_desc(model)
+    u, obs, earth = workload(nside)
+    rng = np.random.default_rng(1234)
+    idx = np.sort(rng.choice(u.shape[1], size=min(n_sample, u.shape[1]), replace=False))
+    us = np.ascontiguousarray(u[:, idx])
+    cores = os.cpu_count() or 1
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        zo.evaluate_chunked(desc, us, obs, earth, nprocesses=cores)
+        times.append(time.perf_counter() - t0)
+    return us.shape[1], cores, times
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+        "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"),
+                stderr=subprocess.DEVNULL,
+            )
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [v.strip() for v in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(rows),
+        }
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n, cores, times = cpu_sample_run(args.nside, CPU_SAMPLE, args.warmup + args.steps)
+    timed = times[args.warmup :]
+    t = sum(timed) / len(timed)
+    v = n / t
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": "LOS/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"DIRBE 25um, HEALPix nside {args.nside}, obspos (0.7071,0.7071,0) AU, GL 50",
+            "sample_los_per_step": n,
+            "l2": "n/a (CPU)",
+        },
+        "cpu_baseline": {
+            "value": v,
+            "unit": "LOS/s",
+            "cores": cores,
+            "kind": "port",
+            "sample": f"{n} seeded random pixels of the nside-{args.nside} map per step, numpy oracle "
+            f"(ZodiPy's per-node vectorised passes) over a {cores}-process fork pool",
+        },
+        "e2e": {"value": v, "unit": "LOS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    rank, world, local_rank = dist_env()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # before any CUDA call: the oracle pool forks
+        n, cores, times = cpu_sample_run(args.nside, CPU_SAMPLE * 2, 1)
+        cpu = {
+            "value": n / times[0],
+            "unit": "LOS/s",
+            "cores": cores,
+            "kind": "port",
+            "sample": f"{n} seeded random pixels of the nside-{args.nside} map, numpy oracle over a {cores}-process fork pool",
+        }
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    from zodipy_gb300 import _build, _lib, engine, packing, roofline
+
+    _build.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    sh = int(stream.cuda_stream)
+
+    model = build_model("float32")
+    zl = model.zl_model
+    u_np, obs, earth = workload(args.nside, rank, world)
+    n = u_np.shape[1]
+    u = torch.from_numpy(u_np).to(dev)
+    table = packing.observer_table(zl, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
+    obs_dev = engine.upload_observers(table, dev)
+    comps = torch.empty((1, zl.n_comps, n), dtype=torch.float64, device=dev)
+    total = torch.empty((1, n), dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step(prec):
+        engine.forward(zl, u, obs_dev, 1, prec, out_comps=comps, out_total=total, stream=sh)
+
+    def timed(prec, k, w):
+        for _ in range(w):
+            step(prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(prec)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    # ---- headline: float32 kernel, inputs resident ---------------------------
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    t32 = timed(_lib.ZL_PREC_F32, args.steps, max(args.warmup, 3))
+    clk = clocks.stop()
+    ms32 = sum(t32) / len(t32)
+    ms_max = torch.tensor([ms32], device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(ms_max, op=torch.distributed.ReduceOp.MAX)
+    ms32_all = float(ms_max.item())
+    comps32 = comps.clone()
+
+    # ---- float64 plain kernel on the same map + error of float32 -------------
+    t64 = timed(_lib.ZL_PREC_F64, max(2, min(args.steps, 3)), 1)
+    ms64 = sum(t64) / len(t64)
+    c64, c32 = comps[0], comps32[0]
+    tot64, tot32 = c64.sum(0), c32.sum(0)
+    e_tot = ((tot32 - tot64).abs() / tot64.abs()).double()
+    floor = torch.maximum(c64.abs(), 1e-3 * tot64.abs()[None, :])
+    e_comp = ((c32 - c64).abs() / floor).amax(dim=1)
+    err = {
+        "total_max": float(e_tot.max()),
+        "total_median": float(e_tot.median()),
+        "component_max": [float(v) for v in e_comp],
+    }
+
+    # ---- XU roofline --------------------------------------------------------
+    sink = torch.empty(8 * 1024, dtype=torch.float32, device=dev)
+    ops = _lib.ctypes.c_double(0)
+
+    def probe(which, iters=2048, reps=5):
+        best = 0.0
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            _lib.check(lib.zl_diag_pipe_probe(which, iters, _lib.ctypes.c_void_p(sink.data_ptr()), sink.numel(), _lib.ctypes.byref(ops), _lib.ctypes.c_void_p(sh)), "probe")
+            b.record(stream)
+            torch.cuda.synchronize()
+            best = max(best, ops.value / (a.elapsed_time(b) * 1e-3))
+        return best
+
+    xu_peak = probe(0)
+    fma_peak = probe(1)
+    xu_per_los = roofline.xu_ops_per_los(zl)
+    xu_achieved = xu_per_los * n / (ms32 * 1e-3)
+
+    # ---- end to end through the public API from pinned host memory ----------
+    u_pinned = torch.from_numpy(u_np).pin_memory()
+    out_pinned = torch.empty(n, dtype=torch.float64).pin_memory()
+    obs_np = np.asarray(obs)
+
+    def e2e_step():
+        res = model.evaluate_xyz(u_pinned, obs_np, earth, return_comps=False, precision="float32", out=out_pinned)
+        return res
+
+    for _ in range(max(args.warmup, 3)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e_t = sum(e2e_ms) / len(e2e_ms)
+
+    peaks = measured_peaks()
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": n * world / (ms32_all * 1e-3),
+            "unit": "LOS/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": max(args.warmup, 3),
+            "ms_per_step": ms32_all,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": f"DIRBE 25um, HEALPix nside {args.nside} ({n} LOS), obspos (0.7071,0.7071,0) AU, GL 50, "
+                "float32-bulk kernel, 6 component maps + total",
+                "l2": "flushed (256 MB write) before every timed step",
+                "parallelism": f"replicas x{world}, no collective on the data path",
+            },
+            "fp64_los_per_s": n / (ms64 * 1e-3),
+            "fp64_ms_per_step": ms64,
+            "speedup_fp32_vs_fp64": ms64 / ms32,
+            "rel_err_fp32_vs_fp64": err,
+            "fwd_bwd_ms": None,
+            "roofline": {
+                "bound": "xu",
+                "achieved": xu_achieved / 1e9,
+                "peak": xu_peak / 1e9,
+                "unit": "Gop/s (MUFU)",
+                "frac": xu_achieved / xu_peak,
+                "traffic": None,
+                "peak_source": "measured: ex2.approx probe kernel (zl_diag_pipe_probe) on this GPU in this run",
+                "xu_ops_per_los": xu_per_los,
+                "fma_peak_gops": fma_peak / 1e9,
+                "hbm_gbs_achieved": roofline.io_bytes_per_los(zl, True, True) * n / (ms32 * 1e-3) / 1e9,
+                "hbm_gbs_peak": peaks.get("hbm_gbs"),
+            },
+            "cpu_baseline": cpu,
+            "e2e": {
+                "value": n / (e2e_t * 1e-3),
+                "unit": "LOS/s",
+                "h2d_bytes_per_step": int(u_np.nbytes) + 64,
+                "d2h_bytes_per_step": int(n * 8),
+            },
+            "gpu_launches": args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

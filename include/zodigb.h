@@ -1,0 +1,162 @@
+/*
+ * zodigb.h — C ABI of the GB300 (sm_103a) zodiacal-light line-of-sight integrator.
+ *
+ * This library replaces the numeric core that ZodiPy runs below
+ * `Model._evaluate` (zodipy/model.py:205-279): the per-component line-of-sight
+ * range (zodipy/line_of_sight.py:64-105), the Gauss-Legendre quadrature
+ * (zodipy/line_of_sight.py:55-61) of the Kelsall integrand
+ * (zodipy/brightness.py:21-56) with the four Kelsall-98 densities
+ * (zodipy/number_density.py:47-181), the blackbody lookup
+ * (zodipy/blackbody.py:16-30 + np.interp) and scattering
+ * (zodipy/scattering.py:11-59).  Everything above that seam (units, frames,
+ * ephemerides, spectral unpacking) stays in the host language.
+ *
+ * Conventions
+ *  - Plain C types only.  Every array argument named *_dev is a CUDA device
+ *    pointer owned by the caller; the library allocates nothing except where
+ *    an entry point says so.
+ *  - `stream` is a cudaStream_t passed as void*; all work is enqueued on it
+ *    and no entry point synchronises.
+ *  - Every entry point returns 0 on success or a negative ZL_ERR_* code; the
+ *    message of the last failure on the calling thread is read with
+ *    zl_last_error().  Nothing aborts the process.
+ */
+#ifndef ZODIGB_H
+#define ZODIGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ZL_API __attribute__((visibility("default")))
+#else
+#define ZL_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZL_ABI_VERSION 1
+
+#define ZL_MAX_COMPS 8   /* components per model (DIRBE has 6) */
+#define ZL_MAX_RANGES 8  /* distinct (inner, outer) cutoff pairs per model */
+#define ZL_MAX_SPEC 4    /* spectral sets (wavelengths / bandpasses) fused in one launch */
+#define ZL_MAX_NODES 128 /* Gauss-Legendre degree */
+#define ZL_MAX_TEMPS 128 /* blackbody table length (the reference uses 100) */
+
+/* Component type codes (zodipy/number_density.py:408-412). */
+enum { ZL_CLOUD = 0, ZL_BAND = 1, ZL_RING = 2, ZL_FEATURE = 3 };
+
+/* Arithmetic of the integrand. */
+enum {
+  ZL_PREC_F64 = 0, /* plain method: float64 throughout, the GPU oracle */
+  ZL_PREC_F32 = 1  /* float32 bulk; float-float geometry near the ring/feature, compensated sums */
+};
+
+enum {
+  ZL_OK = 0,
+  ZL_ERR_ARG = -1,    /* invalid argument (null pointer, size, layout) */
+  ZL_ERR_CUDA = -2,   /* a CUDA runtime call failed */
+  ZL_ERR_MODEL = -3,  /* model description out of range */
+  ZL_ERR_SPACE = -4   /* caller-provided workspace too small */
+};
+
+/* One zodiacal component; geometry derived like zodipy/component.py:39-44. */
+typedef struct ZlComponent {
+  int32_t type;       /* ZL_CLOUD .. ZL_FEATURE */
+  int32_t range;      /* index into ZlModel.cutoff */
+  double offset[3];   /* x_0, y_0, z_0 [AU] */
+  double sin_i, cos_i, sin_Omega, cos_Omega;
+  double n_0;
+  /* cloud:   alpha, beta, gamma, mu
+   * band:    delta_zeta [rad], v, p, delta_r
+   * ring:    R, sigma_r, sigma_z
+   * feature: R, sigma_r, sigma_z, theta [rad], sigma_theta [rad] */
+  double p[6];
+} ZlComponent;
+
+/* Spectral quantities of one wavelength / bandpass
+ * (zodipy/unpack_model.py:23-107, zodipy/blackbody.py:33-49). */
+typedef struct ZlSpectrum {
+  double emissivity[ZL_MAX_COMPS];
+  double albedo[ZL_MAX_COMPS];
+  double C1, C2, C3;           /* phase-function coefficients */
+  double solar_irradiance;     /* [MJy/sr] at 1 AU */
+  double bb[ZL_MAX_TEMPS];     /* blackbody table [MJy/sr] at ZlModel.temps */
+} ZlSpectrum;
+
+/* A complete Kelsall-type model evaluated at ZL_MAX_SPEC or fewer spectral sets. */
+typedef struct ZlModel {
+  int32_t abi_version;         /* = ZL_ABI_VERSION */
+  int32_t n_comps, n_ranges, n_spec, n_nodes, n_temps;
+  double T_0, delta;           /* T(R) = T_0 R^-delta (zodipy/blackbody.py:16-30) */
+  double cutoff[ZL_MAX_RANGES][2]; /* inner, outer cutoff radius [AU] (line_of_sight.py:19-26) */
+  double temps[ZL_MAX_TEMPS];  /* table temperatures [K], uniformly spaced, increasing */
+  double gl_x[ZL_MAX_NODES];   /* Gauss-Legendre nodes on [-1, 1] */
+  double gl_w[ZL_MAX_NODES];   /* Gauss-Legendre weights */
+  ZlComponent comp[ZL_MAX_COMPS];
+  ZlSpectrum spec[ZL_MAX_SPEC];
+} ZlModel;
+
+/* One observer (one instant).  Pixels [pix_begin, next observer's pix_begin)
+ * belong to it; the last observer runs to n_pix.  `outside` is filled by
+ * zl_observer_flags(). */
+typedef struct ZlObserver {
+  double obs[3];      /* heliocentric ecliptic observer position [AU] */
+  double earth[3];    /* heliocentric ecliptic Earth position [AU] */
+  int64_t pix_begin;
+  uint32_t outside;   /* bit 2r: start of range r collapses to eps; bit 2r+1: stop does */
+  uint32_t reserved;
+} ZlObserver;
+
+/* Version of the library (== ZL_ABI_VERSION of the build). */
+ZL_API int zl_abi_version(void);
+
+/* Copy the message of the calling thread's last failure into buf (NUL-terminated). */
+ZL_API int zl_last_error(char* buf, size_t len);
+
+/* Check a model description; returns ZL_OK or ZL_ERR_MODEL with a message. */
+ZL_API int zl_model_check(const ZlModel* model);
+
+/* Fill ZlObserver.outside for n_obs host-side records, reproducing the rule
+ * of zodipy/line_of_sight.py:72-73: a cutoff radius collapses to eps when the
+ * observer lies strictly outside that sphere.  With any_mode != 0 the flags of
+ * all records are OR-ed together, which is the reference's behaviour when one
+ * call carries a position per pixel (time-ordered data). */
+ZL_API int zl_observer_flags(const ZlModel* model, ZlObserver* obs_host, int64_t n_obs, int32_t any_mode);
+
+/* Forward pass: the emission of every component at every pixel.
+ * Replaces model.py:253-277 (and the sum of model.py:203).
+ *  unit_vectors_dev: float64 [3][n_pix], heliocentric-ecliptic unit vectors (SoA)
+ *  observers_dev:    n_obs ZlObserver records sorted by pix_begin, first = 0
+ *  out_comps_dev:    float64 [n_spec][n_comps][n_pix] or NULL
+ *  out_total_dev:    float64 [n_spec][n_pix] or NULL; the component sum in
+ *                    component order, so it equals out_comps summed over axis 0
+ *  precision:        ZL_PREC_F64 or ZL_PREC_F32 */
+ZL_API int zl_forward(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+               const ZlObserver* observers_dev, int32_t n_obs, int32_t precision,
+               double* out_comps_dev, double* out_total_dev, void* stream);
+
+/* Launch configuration used by zl_forward for a precision, as chosen by the
+ * autotuner (threads per block, blocks per SM; 0 = library default). */
+ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);
+
+/* Diagnostics (not needed by callers): 1 selects an all-float32 geometry
+ * variant of the DIRBE-layout float32 kernel, used to measure what the
+ * float-float ring/feature geometry buys.  Applies to later zl_forward calls
+ * of every thread. */
+ZL_API int zl_debug_plain_geometry(int32_t on);
+
+/* Diagnostics: launch a pipe-throughput probe on `stream` (which = 0: MUFU
+ * ex2, which = 1: FP32 FMA), `iters` iterations of 8 independent chains per
+ * thread; *ops_per_launch receives the number of probe instructions.  The
+ * caller times the launch.  sink_dev must hold >= 8 * SM-count floats. */
+ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int32_t sink_len,
+                              double* ops_per_launch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ZODIGB_H */

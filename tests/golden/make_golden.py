@@ -1,0 +1,229 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Run in a checkout where the ZodiPy v1.1.3 source tree is available (default
+/root/reference, override with ZODIPY_REF_ROOT):
+
+    python tests/golden/make_golden.py
+
+The reference's own numeric modules are executed in place under an astropy
+stand-in (oracle/ref_loader.py).  Inputs that the reference would get from
+astropy — unit vectors, Earth/observer positions, the blackbody table — are
+built here and stored with the outputs, so the fixtures pin the path from
+those inputs to the per-component emission.  Outputs:
+
+  ref_models.json     parameter dictionaries of the reference's Kelsall models
+  spectral.json       spectral scalars from the reference's interp_spectral_param
+  los_<case>.npz      inputs + reference per-component emission for one call
+  dirbe_idl.npz       inputs + reference emission for the DIRBE IDL known-answer
+                      points (tests/dirbe_tabulated.py of the reference)
+"""
+
+from __future__ import annotations
+
+import ast
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle import zodi_oracle  # noqa: E402
+from oracle.ref_loader import DEFAULT_REF_ROOT, load_reference, reference_evaluate, reference_spectral_scalars  # noqa: E402
+from zodipy_gb300.ephemeris import earth_position, iso_to_mjd  # noqa: E402
+from zodipy_gb300.healpix import pix2vec_ring, random_sphere  # noqa: E402
+
+C_UM_GHZ = 299792.458  # nu[GHz] = C / lambda[um]
+
+
+def dump_models(ref) -> dict:
+    out = {}
+    reg = ref.model_registry.model_registry
+    for name in reg.models:
+        m = reg.get_model(name)
+        if type(m).__name__ != "Kelsall":
+            continue
+        d = m.to_dict()
+
+        def seq(v):
+            return None if v is None else [float(x) for x in v]
+
+        out[name] = {
+            "comps": {k: {kk: float(vv) for kk, vv in v.items()} for k, v in d["comps"].items()},
+            "spectrum": seq(np.asarray(m.spectrum)),
+            "spectrum_unit": "micron" if name == "dirbe" else "GHz",
+            "T_0": float(d["T_0"]),
+            "delta": float(d["delta"]),
+            "emissivities": {k: seq(v) for k, v in d["emissivities"].items()},
+            "albedos": None if d["albedos"] is None else {k: seq(v) for k, v in d["albedos"].items()},
+            "solar_irradiance": seq(d["solar_irradiance"]),
+            "C1": seq(d["C1"]),
+            "C2": seq(d["C2"]),
+            "C3": seq(d["C3"]),
+            "cutoffs": {
+                lbl.value: [float(v) for v in ref.line_of_sight.COMPONENT_CUTOFFS[lbl]] for lbl in m.comps
+            },
+        }
+    return out
+
+
+def model_unit(name: str) -> str:
+    return "micron" if name == "dirbe" else "GHz"
+
+
+def to_model_units(x, user_unit: str, name: str) -> np.ndarray:
+    x = np.asarray(x, dtype=np.float64)
+    if user_unit == model_unit(name):
+        return x
+    return C_UM_GHZ / x
+
+
+def make_case(ref, name, x, user_unit, weights, u, obs, earth, degree):
+    """Run the reference for one call; returns the npz payload."""
+    w_norm = None
+    if weights is not None:
+        w = np.asarray(weights, dtype=np.float64)
+        w_norm = w / np.trapezoid(w, np.asarray(x, dtype=np.float64))
+    bb = zodi_oracle.planck_table(x, w_norm, unit=user_unit)
+    xm = to_model_units(x, user_unit, name)
+    out = reference_evaluate(ref, name, u, obs, earth, bb, xm, w_norm, degree, bounds_error=False)
+    scal = reference_spectral_scalars(ref, name, xm, w_norm, bounds_error=False)
+    return dict(
+        model=np.array(name),
+        x=np.atleast_1d(np.asarray(x, dtype=np.float64)),
+        x_is_scalar=np.array(weights is None),
+        user_unit=np.array(user_unit),
+        weights=np.zeros(0) if weights is None else np.asarray(weights, dtype=np.float64),
+        unit_vectors=np.asarray(u, dtype=np.float64),
+        obs=np.asarray(obs, dtype=np.float64),
+        earth=np.asarray(earth, dtype=np.float64),
+        bb_table=bb,
+        degree=np.array(degree),
+        emissivity=np.array(scal["emissivity"]),
+        albedo=np.array(scal["albedo"]),
+        C=np.array([scal["C1"], scal["C2"], scal["C3"], scal["solar_irradiance"]]),
+        ref_out=out,
+    )
+
+
+def dirbe_idl_fixture(ref_root: str):
+    """DAYS/LON/LAT/TABULATED_DIRBE_EMISSION read as literals from the reference's test data."""
+    path = os.path.join(ref_root, "tests", "dirbe_tabulated.py")
+    tree = ast.parse(open(path).read())
+    vals = {}
+    for node in tree.body:
+        if isinstance(node, (ast.Assign, ast.AnnAssign)):
+            target = node.targets[0] if isinstance(node, ast.Assign) else node.target
+            if isinstance(target, ast.Name) and target.id in ("DAYS", "LON", "LAT", "TABULATED_DIRBE_EMISSION"):
+                vals[target.id] = ast.literal_eval(node.value)
+    return vals
+
+
+def main() -> None:
+    ref_root = os.environ.get("ZODIPY_REF_ROOT", DEFAULT_REF_ROOT)
+    ref = load_reference(ref_root)
+    models = dump_models(ref)
+    with open(os.path.join(HERE, "ref_models.json"), "w") as f:
+        json.dump(models, f, indent=1)
+
+    # spectral scalars for a spread of inputs (delta, bandpass, GHz input, extrapolation)
+    spec_cases = {
+        "dirbe_25um": ("dirbe", 25.0, "micron", None),
+        "dirbe_1p25um": ("dirbe", 1.25, "micron", None),
+        "dirbe_3p1um": ("dirbe", 3.1, "micron", None),
+        "dirbe_20um_as_ghz": ("dirbe", C_UM_GHZ / 20.0, "GHz", None),
+        "dirbe_300um_extrap": ("dirbe", 300.0, "micron", None),
+        "planck18_857ghz": ("planck18", 857.0, "GHz", None),
+        "planck13_600ghz": ("planck13", 600.0, "GHz", None),
+        "dirbe_bp_80_130": ("dirbe", list(np.linspace(80, 130, 64)), "micron", list(np.exp(-0.5 * ((np.linspace(80, 130, 64) - 100) / 10) ** 2))),
+        "dirbe_bp_1_3": ("dirbe", list(np.linspace(1.1, 3.0, 17)), "micron", list(np.linspace(0.2, 1.0, 17))),
+    }
+    spectral = {}
+    for key, (name, x, unit, w) in spec_cases.items():
+        xa = np.asarray(x, dtype=np.float64)
+        w_norm = None if w is None else np.asarray(w) / np.trapezoid(np.asarray(w), xa)
+        xm = to_model_units(xa, unit, name)
+        spectral[key] = {
+            "model": name,
+            "x": xa.tolist() if xa.ndim else float(xa),
+            "unit": unit,
+            "weights": w,
+            "scalars": reference_spectral_scalars(ref, name, xm, w_norm, bounds_error=False),
+            "bb_table": zodi_oracle.planck_table(xa, w_norm, unit=unit).tolist(),
+        }
+    with open(os.path.join(HERE, "spectral.json"), "w") as f:
+        json.dump(spectral, f, indent=1)
+
+    rng = np.random.default_rng(20240611)
+    earth_2022 = earth_position(iso_to_mjd("2022-01-01T00:00:00"))
+    earth_1990 = earth_position(iso_to_mjd("1990-06-11T00:00:00"))
+    dirs_hp8 = pix2vec_ring(8)
+    dirs_rand = random_sphere(256, seed=7)
+    cases = {
+        "dirbe25_nside8": ("dirbe", 25.0, "micron", None, dirs_hp8, [0.9833, 0.0, 0.0], earth_2022, 50),
+        "dirbe1p25_scatter": ("dirbe", 1.25, "micron", None, dirs_rand, earth_1990, earth_1990, 50),
+        "dirbe3p5_scatter": ("dirbe", 3.5, "micron", None, dirs_rand, [0.0, 1.01, 0.002], earth_1990, 50),
+        "planck18_857": ("planck18", 857.0, "GHz", None, dirs_rand, [np.cos(2.0), np.sin(2.0), 0.013], earth_2022, 50),
+        "planck13_545": ("planck13", 545.0, "GHz", None, dirs_rand, [0.3, -0.95, 0.0], earth_2022, 50),
+        "odegard_353": ("odegard", 353.0, "GHz", None, dirs_rand, [-0.98, 0.2, -0.01], earth_2022, 50),
+        "dirbe_bandpass": (
+            "dirbe",
+            np.linspace(80, 130, 64),
+            "micron",
+            np.exp(-0.5 * ((np.linspace(80, 130, 64) - 100) / 10) ** 2),
+            dirs_rand,
+            [0.7071, 0.7071, 0.0],
+            earth_2022,
+            50,
+        ),
+        "dirbe12_gl100": ("dirbe", 12.0, "micron", None, dirs_rand, [0.9833, 0.0, 0.0], earth_2022, 100),
+        "dirbe25_mars": ("dirbe", 25.0, "micron", None, dirs_rand, [1.1, -1.1, 0.03], earth_2022, 50),
+        "dirbe25_venus": ("dirbe", 25.0, "micron", None, dirs_rand, [0.5, 0.5, 0.01], earth_2022, 50),
+        "dirbe60_gl7": ("dirbe", 60.0, "micron", None, dirs_rand, [0.2, 0.99, 0.0], earth_2022, 7),
+        "dirbe25_b0": ("dirbe", 25.0, "micron", None, dirs_rand[:, :32], [0.0, 0.0, 0.4], earth_2022, 20),
+        "dirbe25_single": ("dirbe", 25.0, "micron", None, dirs_rand[:, :1], [0.9833, 0.0, 0.0], earth_2022, 50),
+    }
+    for key, (name, x, unit, w, u, obs, earth, deg) in cases.items():
+        payload = make_case(ref, name, x, unit, w, u, np.asarray(obs, dtype=np.float64), earth, deg)
+        np.savez_compressed(os.path.join(HERE, f"los_{key}.npz"), **payload)
+
+    # time-ordered data: a position per pixel (3, N), as the reference takes for obstime.size > 1
+    n_tod = 128
+    t = np.linspace(0.0, 2.0 * np.pi, n_tod)
+    obs_tod = np.stack([np.cos(t), np.sin(t), 0.01 * np.sin(3 * t)])
+    earth_tod = np.stack([np.cos(t + 0.01), np.sin(t + 0.01), np.zeros(n_tod)])
+    payload = make_case(ref, "dirbe", 25.0, "micron", None, random_sphere(n_tod, seed=11), obs_tod, earth_tod, 50)
+    np.savez_compressed(os.path.join(HERE, "los_dirbe25_tod.npz"), **payload)
+
+    # DIRBE IDL known-answer points (observer = Earth, approximate ephemeris)
+    kat = dirbe_idl_fixture(ref_root)
+    start = iso_to_mjd("1990-01-01T00:00:00")
+    lon, lat = np.radians(kat["LON"]), np.radians(kat["LAT"])
+    u = np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)])
+    mjd = start + np.asarray(kat["DAYS"], dtype=np.float64) - 1.0
+    earth = earth_position(mjd)
+    bands = sorted(kat["TABULATED_DIRBE_EMISSION"])
+    ref_tot = np.zeros((len(bands), len(mjd)))
+    tab = np.zeros_like(ref_tot)
+    for bi, band in enumerate(bands):
+        for j in range(len(mjd)):
+            p = make_case(ref, "dirbe", float(band), "micron", None, u[:, j : j + 1], earth[:, j], earth[:, j], 50)
+            ref_tot[bi, j] = p["ref_out"].sum(axis=0)[0]
+        tab[bi] = kat["TABULATED_DIRBE_EMISSION"][band]
+    np.savez_compressed(
+        os.path.join(HERE, "dirbe_idl.npz"),
+        bands=np.asarray(bands, dtype=np.float64),
+        unit_vectors=u,
+        earth=earth,
+        mjd=mjd,
+        ref_total=ref_tot,
+        tabulated=tab,
+    )
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,309 @@
+// C ABI of the line-of-sight integrator (declared in include/zodigb.h).
+//
+// Host code only: argument validation, derivation of the per-launch kernel
+// parameter blocks from a ZlModel, and kernel launch on the caller's stream.
+// No entry point allocates device memory or synchronises.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "zl_common.cuh"
+
+namespace zl {
+cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ZlObserver* obs, int n_obs,
+                           double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
+cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
+                           const ZlObserver* obs, int n_obs, double* oc, double* ot, cudaStream_t st, int tpb,
+                           int bps, int num_sms);
+}  // namespace zl
+
+using namespace zl;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(ZL_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+struct LaunchCfg {
+  int tpb = 128;
+  int bps = 0;  // 0 = derived from occupancy
+};
+LaunchCfg g_cfg[2];
+std::mutex g_mu;
+
+int sm_count(int* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(out, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  return ZL_OK;
+}
+
+bool is_finite(double x) { return std::isfinite(x); }
+
+void split(double d, float* hi, float* lo) {
+  *hi = (float)d;
+  *lo = (float)(d - (double)*hi);
+}
+
+}  // namespace
+
+extern "C" ZL_API int zl_abi_version(void) { return ZL_ABI_VERSION; }
+
+extern "C" ZL_API int zl_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return ZL_ERR_ARG;
+  strncpy(buf, g_err, len - 1);
+  buf[len - 1] = '\0';
+  return ZL_OK;
+}
+
+extern "C" ZL_API int zl_model_check(const ZlModel* m) {
+  if (!m) return fail(ZL_ERR_ARG, "model is NULL");
+  if (m->abi_version != ZL_ABI_VERSION)
+    return fail(ZL_ERR_MODEL, "model abi_version %d != library %d", m->abi_version, ZL_ABI_VERSION);
+  if (m->n_comps < 1 || m->n_comps > ZL_MAX_COMPS) return fail(ZL_ERR_MODEL, "n_comps=%d out of [1,%d]", m->n_comps, ZL_MAX_COMPS);
+  if (m->n_ranges < 1 || m->n_ranges > ZL_MAX_RANGES) return fail(ZL_ERR_MODEL, "n_ranges=%d out of [1,%d]", m->n_ranges, ZL_MAX_RANGES);
+  if (m->n_spec < 1 || m->n_spec > ZL_MAX_SPEC) return fail(ZL_ERR_MODEL, "n_spec=%d out of [1,%d]", m->n_spec, ZL_MAX_SPEC);
+  if (m->n_nodes < 1 || m->n_nodes > ZL_MAX_NODES) return fail(ZL_ERR_MODEL, "n_nodes=%d out of [1,%d]", m->n_nodes, ZL_MAX_NODES);
+  if (m->n_temps < 2 || m->n_temps > ZL_MAX_TEMPS) return fail(ZL_ERR_MODEL, "n_temps=%d out of [2,%d]", m->n_temps, ZL_MAX_TEMPS);
+  for (int t = 1; t < m->n_temps; ++t)
+    if (!(m->temps[t] > m->temps[t - 1])) return fail(ZL_ERR_MODEL, "temps must increase (index %d)", t);
+  const double dt = (m->temps[m->n_temps - 1] - m->temps[0]) / (m->n_temps - 1);
+  for (int t = 0; t < m->n_temps; ++t)
+    if (std::fabs(m->temps[t] - (m->temps[0] + t * dt)) > 1e-9 * std::fabs(m->temps[m->n_temps - 1]))
+      return fail(ZL_ERR_MODEL, "temps must be uniformly spaced (index %d)", t);
+  for (int c = 0; c < m->n_comps; ++c) {
+    const ZlComponent& C = m->comp[c];
+    if (C.type < ZL_CLOUD || C.type > ZL_FEATURE) return fail(ZL_ERR_MODEL, "component %d: bad type %d", c, C.type);
+    if (C.range < 0 || C.range >= m->n_ranges) return fail(ZL_ERR_MODEL, "component %d: range %d out of [0,%d)", c, C.range, m->n_ranges);
+  }
+  for (int r = 0; r < m->n_ranges; ++r)
+    if (!(m->cutoff[r][0] >= 0.0) || !is_finite(m->cutoff[r][1]) || !(m->cutoff[r][1] > 0.0))
+      return fail(ZL_ERR_MODEL, "range %d: bad cutoffs (%g, %g)", r, m->cutoff[r][0], m->cutoff[r][1]);
+  return ZL_OK;
+}
+
+extern "C" ZL_API int zl_observer_flags(const ZlModel* m, ZlObserver* obs, int64_t n_obs, int32_t any_mode) {
+  int rc = zl_model_check(m);
+  if (rc) return rc;
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  uint32_t all = 0;
+  for (int64_t o = 0; o < n_obs; ++o) {
+    const double* p = obs[o].obs;
+    // line_of_sight.py:71-73
+    const double r_obs = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    uint32_t f = 0;
+    for (int r = 0; r < m->n_ranges; ++r) {
+      if (r_obs > m->cutoff[r][0]) f |= 1u << (2 * r);
+      if (r_obs > m->cutoff[r][1]) f |= 1u << (2 * r + 1);
+    }
+    obs[o].outside = f;
+    all |= f;
+  }
+  if (any_mode)
+    for (int64_t o = 0; o < n_obs; ++o) obs[o].outside = all;
+  return ZL_OK;
+}
+
+extern "C" ZL_API int zl_set_launch(int32_t precision, int32_t tpb, int32_t bps) {
+  if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
+  if (tpb != 0 && (tpb < 32 || tpb > 128 || tpb % 32)) return fail(ZL_ERR_ARG, "threads_per_block %d not in {32..128 step 32}", tpb);
+  if (bps < 0 || bps > 64) return fail(ZL_ERR_ARG, "blocks_per_sm %d out of [0,64]", bps);
+  std::lock_guard<std::mutex> g(g_mu);
+  g_cfg[precision].tpb = tpb ? tpb : 128;
+  g_cfg[precision].bps = bps;
+  return ZL_OK;
+}
+
+namespace {
+
+void first_in_range(const ZlModel& m, int32_t* out) {
+  for (int c = 0; c < m.n_comps; ++c) out[c] = (c == 0 || m.comp[c].range != m.comp[c - 1].range) ? 1 : 0;
+}
+
+// 1 = DIRBE-like (cloud | 3 bands on one range | ring | feature), 2 = Planck-like, 0 = generic
+int detect_layout(const ZlModel& m) {
+  int32_t first[ZL_MAX_COMPS];
+  first_in_range(m, first);
+  static const int dirbe_t[6] = {ZL_CLOUD, ZL_BAND, ZL_BAND, ZL_BAND, ZL_RING, ZL_FEATURE};
+  static const int dirbe_f[6] = {1, 0, 0, 0, 1, 1};
+  if (m.n_comps == 6) {
+    bool ok = true;
+    for (int c = 0; c < 6; ++c) ok = ok && m.comp[c].type == dirbe_t[c] && first[c] == dirbe_f[c];
+    if (ok) return 1;
+  }
+  if (m.n_comps == 4) {
+    bool ok = true;
+    for (int c = 0; c < 4; ++c) ok = ok && m.comp[c].type == dirbe_t[c] && first[c] == dirbe_f[c];
+    if (ok) return 2;
+  }
+  return 0;
+}
+
+void build_f64(const ZlModel& m, KParamsF64* P) {
+  memset(P, 0, sizeof(*P));
+  P->m = m;
+  for (int s = 0; s < m.n_spec; ++s) {
+    for (int t = 0; t + 1 < m.n_temps; ++t)
+      P->slope[s][t] = (m.spec[s].bb[t + 1] - m.spec[s].bb[t]) / (m.temps[t + 1] - m.temps[t]);
+    const double C1 = m.spec[s].C1, C2 = m.spec[s].C2, C3 = m.spec[s].C3;
+    // scattering.py:53-59
+    const double t1 = 2 * M_PI, t2 = 2 * C1, t3 = M_PI * C2, t4 = (std::exp(C3 * M_PI) + 1) / (C3 * C3 + 1);
+    P->phase_norm[s] = 1 / (t1 * (t2 + t3 + t4));
+  }
+  first_in_range(m, P->first_in_range);
+  for (int c = 0; c < m.n_comps; ++c)
+    for (int s = 0; s < m.n_spec; ++s)
+      if (m.spec[s].albedo[c] != 0.0) P->range_scat[m.comp[c].range] = 1;
+}
+
+void build_f32(const ZlModel& m, KParamsF32* P) {
+  memset(P, 0, sizeof(*P));
+  const double L2E = 1.4426950408889634;
+  P->n_comps = m.n_comps;
+  P->n_ranges = m.n_ranges;
+  P->n_spec = m.n_spec;
+  P->n_nodes = m.n_nodes;
+  P->n_temps = m.n_temps;
+  P->T0 = (float)m.T_0;
+  P->neg_delta = (float)(-m.delta);
+  P->t_min = (float)m.temps[0];
+  P->t_max = (float)m.temps[m.n_temps - 1];
+  P->inv_dt = (float)((m.n_temps - 1) / (m.temps[m.n_temps - 1] - m.temps[0]));
+  for (int r = 0; r < m.n_ranges; ++r) {
+    P->cut_in[r] = m.cutoff[r][0];
+    P->cut_out[r] = m.cutoff[r][1];
+    split(m.cutoff[r][0] * m.cutoff[r][0], &P->cut_in_hi[r], &P->cut_in_lo[r]);
+    split(m.cutoff[r][1] * m.cutoff[r][1], &P->cut_out_hi[r], &P->cut_out_lo[r]);
+  }
+  for (int k = 0; k < m.n_nodes; ++k) {
+    split(m.gl_x[k], &P->gl_x_hi[k], &P->gl_x_lo[k]);
+    P->gl_w[k] = (float)m.gl_w[k];
+  }
+  int32_t first[ZL_MAX_COMPS];
+  first_in_range(m, first);
+  for (int c = 0; c < m.n_comps; ++c) {
+    const ZlComponent& C = m.comp[c];
+    KCompF32& K = P->comp[c];
+    K.type = C.type;
+    K.range = C.range;
+    K.first_in_range = first[c];
+    K.zero_offset = (C.offset[0] == 0.0 && C.offset[1] == 0.0 && C.offset[2] == 0.0) ? 1 : 0;
+    K.nx = (float)(C.sin_Omega * C.sin_i);
+    K.ny = (float)(-C.cos_Omega * C.sin_i);
+    K.nz = (float)C.cos_i;
+    split(C.offset[0], &K.ox, &K.ox_lo);
+    split(C.offset[1], &K.oy, &K.oy_lo);
+    split(C.offset[2], &K.oz, &K.oz_lo);
+    const double* p = C.p;
+    switch (C.type) {
+      case ZL_CLOUD:
+        K.c[0] = (float)C.n_0;
+        K.c[1] = (float)p[0];
+        K.c[2] = (float)(p[1] * L2E);
+        K.c[3] = (float)p[2];
+        K.c[4] = (float)p[3];
+        K.c[5] = (float)(1.0 / (2.0 * p[3]));
+        K.c[6] = (float)(p[3] / 2.0);
+        break;
+      case ZL_BAND:
+        K.c[0] = (float)(3.0 * C.n_0);
+        K.c[1] = (float)(1.0 / p[0]);
+        K.c[2] = (float)(1.0 / p[1]);
+        K.c[3] = (float)p[2];
+        K.c[4] = (float)(1.0 / (p[3] * p[3]));
+        K.c[5] = (p[2] == 4.0) ? 1.0f : 0.0f;
+        break;
+      case ZL_RING:
+      case ZL_FEATURE:
+        K.c[0] = (float)C.n_0;
+        K.c[1] = (float)p[0];
+        K.c[2] = (float)(L2E / (p[1] * p[1]));
+        K.c[3] = (float)(L2E / p[2]);
+        split(p[0] * p[0], &K.c[4], &K.c[5]);
+        if (C.type == ZL_FEATURE) {
+          K.c[6] = (float)p[3];
+          K.c[7] = (float)(L2E / (p[4] * p[4]));
+        }
+        break;
+    }
+  }
+  for (int s = 0; s < m.n_spec; ++s) {
+    const ZlSpectrum& S = m.spec[s];
+    KSpecF32& K = P->spec[s];
+    for (int c = 0; c < m.n_comps; ++c) {
+      K.em1[c] = (float)((1.0 - S.albedo[c]) * S.emissivity[c]);
+      K.alb[c] = (float)S.albedo[c];
+      if (S.albedo[c] != 0.0) P->has_scat = 1;
+    }
+    const double t1 = 2 * M_PI, t2 = 2 * S.C1, t3 = M_PI * S.C2, t4 = (std::exp(S.C3 * M_PI) + 1) / (S.C3 * S.C3 + 1);
+    K.C1 = (float)S.C1;
+    K.C2 = (float)S.C2;
+    K.C3l2e = (float)(S.C3 * L2E);
+    K.S = (float)S.solar_irradiance;
+    K.N = (float)(1 / (t1 * (t2 + t3 + t4)));
+    for (int t = 0; t < m.n_temps; ++t) {
+      const double slope = (t + 1 < m.n_temps) ? (S.bb[t + 1] - S.bb[t]) / (m.temps[t + 1] - m.temps[t]) : 0.0;
+      P->table[s][t] = make_float4((float)m.temps[t], (float)S.bb[t], (float)slope, 0.f);
+    }
+  }
+}
+
+}  // namespace
+
+// Testing hook: 1 selects the all-float32 geometry variant of the DIRBE-layout
+// kernel (no float-float near the ring and feature).  Not part of the ABI.
+static int g_plain_geometry = 0;
+extern "C" ZL_API int zl_debug_plain_geometry(int32_t on) {
+  g_plain_geometry = on ? 1 : 0;
+  return ZL_OK;
+}
+
+extern "C" ZL_API int zl_forward(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs, int32_t n_obs,
+                          int32_t precision, double* out_comps, double* out_total, void* stream) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
+  if (n_pix == 0) return ZL_OK;
+  if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  if (!out_comps && !out_total) return fail(ZL_ERR_ARG, "both outputs are NULL");
+  if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
+  int nsm = 0;
+  if ((rc = sm_count(&nsm))) return rc;
+  LaunchCfg cfg;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    cfg = g_cfg[precision];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (precision == ZL_PREC_F64) {
+    static thread_local KParamsF64 P;
+    build_f64(*model, &P);
+    const int bps = cfg.bps ? cfg.bps : 8;
+    e = launch_fwd_f64(P, u, n_pix, obs, n_obs, out_comps, out_total, st, cfg.tpb, bps, nsm);
+  } else {
+    static thread_local KParamsF32 P;
+    build_f32(*model, &P);
+    const int bps = cfg.bps ? cfg.bps : 8;
+    e = launch_fwd_f32(P, detect_layout(*model), g_plain_geometry != 0, u, n_pix, obs, n_obs, out_comps, out_total,
+                       st, cfg.tpb, bps, nsm);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "zl_forward launch");
+  return ZL_OK;
+}

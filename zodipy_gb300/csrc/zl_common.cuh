@@ -1,0 +1,176 @@
+// Device-side building blocks shared by the forward and adjoint kernels.
+//
+// The kernels evaluate ZodiPy's line-of-sight integral (zodipy/model.py:253-277):
+// for every pixel and component, a Gauss-Legendre sum over the Kelsall integrand
+// (zodipy/brightness.py:21-56) between the cutoff-sphere intersections
+// (zodipy/line_of_sight.py:64-105).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/zodigb.h"
+
+namespace zl {
+
+constexpr double kEps = 2.220446049250313e-16;  // np.finfo(float64).eps (line_of_sight.py:14)
+constexpr double kPi = 3.141592653589793;
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kPiF = 3.14159265358979f;
+constexpr float kTwoPiF = 6.28318530717959f;
+constexpr float kInvTwoPiF = 0.159154943091895f;
+
+// ---------------------------------------------------------------------------
+// Host-derived kernel parameter blocks.  They are built once per launch from a
+// ZlModel by the host code in zl_api.cu and passed by value (__grid_constant__),
+// so concurrent launches with different models never share state.
+// ---------------------------------------------------------------------------
+
+// float64 plain kernel: the model itself plus slopes of the blackbody table.
+struct KParamsF64 {
+  ZlModel m;
+  double slope[ZL_MAX_SPEC][ZL_MAX_TEMPS];  // (fp[j+1]-fp[j])/(xp[j+1]-xp[j]) as np.interp forms it
+  double phase_norm[ZL_MAX_SPEC];           // scattering.py:53-59
+  int32_t first_in_range[ZL_MAX_COMPS];     // component starts a new LOS range group
+  int32_t range_scat[ZL_MAX_RANGES];        // some component of the range has albedo != 0
+};
+
+// Per-component constants of the float32 kernel (Kelsall-98 densities).
+struct KCompF32 {
+  int32_t type, range, first_in_range, zero_offset;
+  float nx, ny, nz;        // unit normal of the symmetry plane (sinO sini, -cosO sini, cosi)
+  float ox, oy, oz;        // offset X_0 [AU]
+  float ox_lo, oy_lo, oz_lo;  // low parts of X_0 for float-float geometry
+  // type constants:
+  //  cloud:   c0=n_0, c1=alpha, c2=beta*log2(e), c3=gamma, c4=mu, c5=1/(2 mu), c6=mu/2
+  //  band:    c0=3 n_0, c1=1/delta_zeta_rad, c2=1/v, c3=p, c4=1/delta_r^2, c5=(p==4)
+  //  ring:    c0=n_0, c1=R, c2=log2(e)/sigma_r^2, c3=log2(e)/sigma_z, c4=R^2 (hi), c5=R^2 (lo)
+  //  feature: c0=n_0, c1=R, c2=log2(e)/sigma_r^2, c3=log2(e)/sigma_z, c4=R^2 (hi), c5=R^2 (lo),
+  //           c6=theta_rad, c7=log2(e)/sigma_theta_rad^2
+  float c[8];
+};
+
+struct KSpecF32 {
+  float em1[ZL_MAX_COMPS];  // (1 - albedo) * emissivity
+  float alb[ZL_MAX_COMPS];  // albedo
+  float C1, C2, C3l2e, S, N;  // phase function (C3 pre-multiplied by log2 e), solar flux, normalisation
+  float pad[3];
+};
+
+struct KParamsF32 {
+  int32_t n_comps, n_ranges, n_spec, n_nodes, n_temps, has_scat;
+  float T0, neg_delta, t_min, t_max, inv_dt, pad0;
+  double cut_in[ZL_MAX_RANGES], cut_out[ZL_MAX_RANGES];
+  float cut_in_hi[ZL_MAX_RANGES], cut_in_lo[ZL_MAX_RANGES];
+  float cut_out_hi[ZL_MAX_RANGES], cut_out_lo[ZL_MAX_RANGES];
+  float gl_x_hi[ZL_MAX_NODES], gl_x_lo[ZL_MAX_NODES], gl_w[ZL_MAX_NODES];
+  KCompF32 comp[ZL_MAX_COMPS];
+  KSpecF32 spec[ZL_MAX_SPEC];
+  float4 table[ZL_MAX_SPEC][ZL_MAX_TEMPS];  // (T_j, B_j, slope_j, 0), staged to shared memory
+};
+
+// ---------------------------------------------------------------------------
+// Float-float ("double-single") arithmetic on the FP32 pipe.  GB300 runs FP64
+// at a small fraction of its FP32 rate, so the few quantities that need more
+// than 24 bits (cutoff intersections, node positions near the ring and the
+// feature) carry a (hi, lo) pair with ~48-bit significand instead.
+// Algorithms: Dekker (1971) / Knuth TwoSum, FMA-based TwoProd.
+// ---------------------------------------------------------------------------
+struct ff {
+  float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+
+__device__ __forceinline__ ff ff_quick(float a, float b) {  // |a| >= |b|
+  float s = a + b;
+  float e = b - (s - a);
+  return {s, e};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = ff_two_sum(a.hi, b.hi);
+  ff t = ff_two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = ff_quick(s.hi, s.lo);
+  s.lo += t.lo;
+  return ff_quick(s.hi, s.lo);
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ff_quick(p, e);
+}
+
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+  float p = a.hi * b;
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  return ff_quick(p, e);
+}
+
+// a * b + c, all float-float
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
+
+__device__ __forceinline__ ff ff_scale(ff a, float pow2) { return {a.hi * pow2, a.lo * pow2}; }
+
+__device__ __forceinline__ ff ff_from_double(double d) {
+  float hi = __double2float_rn(d);
+  float lo = __double2float_rn(d - (double)hi);
+  return {hi, lo};
+}
+
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+// sqrt of a positive float-float (one Newton correction of the FP32 root)
+__device__ __forceinline__ ff ff_sqrt(ff a) {
+  if (!(a.hi > 0.f)) return {sqrtf(a.hi), 0.f};
+  float r = rsqrtf(a.hi);
+  float s = a.hi * r;
+  ff s2 = {s * s, fmaf(s, s, -s * s)};
+  ff d = ff_add(a, ff_neg(s2));
+  return ff_quick(s, d.hi * 0.5f * r);
+}
+
+// a / b (one Newton correction)
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  float q = a.hi / b.hi;
+  ff p = ff_mulf(b, q);
+  ff r = ff_add(a, ff_neg(p));
+  return ff_quick(q, r.hi / b.hi);
+}
+
+// floor of a non-negative float below 2^22 without the conversion pipe
+__device__ __forceinline__ int floor_nonneg(float t) {
+  float m = t + 8388608.0f;  // 2^23: the mantissa now holds round(t)
+  int j = __float_as_int(m) - 0x4B000000;
+  float r = m - 8388608.0f;
+  return j - (r > t ? 1 : 0);
+}
+
+// ---------------------------------------------------------------------------
+// Binary search of the observer that owns pixel `i` (records sorted by pix_begin).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_observer(const ZlObserver* __restrict__ obs, int n_obs, int64_t i) {
+  int lo = 0, hi = n_obs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&obs[mid].pix_begin) <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace zl

@@ -1,0 +1,67 @@
+// Pipe-throughput probes used as roofline denominators.
+//
+// The line-of-sight kernels are bound by the MUFU (XU) pipe and the FP32 FMA
+// pipe, neither of which has a vendor-measured peak in the benchmark inputs, so
+// the benchmark measures both with these kernels on the same GPU and clock:
+//  - which = 0: ex2.approx.ftz.f32 (one MUFU op each), 8 independent chains per thread
+//  - which = 1: fma.rn.f32 (one FFMA each), 8 independent chains per thread
+// Every result feeds a store guarded by an impossible condition so the chains
+// are not removed.
+#include <cuda_runtime.h>
+
+#include "../../include/zodigb.h"
+
+namespace {
+
+__global__ void __launch_bounds__(256) xu_probe(float* sink, int iters, float seed) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = seed * (float)(threadIdx.x + j) * 1e-9f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float r;
+      asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a[j]));
+      a[j] = r * -1e-3f;
+    }
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == 1234.5f) sink[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) fma_probe(float* sink, int iters, float seed) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = seed + (float)(threadIdx.x + j);
+  const float m = 0.999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fmaf(a[j], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == 1234.5f) sink[blockIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int32_t sink_len,
+                                         double* ops_per_launch, void* stream) {
+  if ((which != 0 && which != 1) || iters < 1 || !sink_dev || !ops_per_launch) return ZL_ERR_ARG;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return ZL_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ZL_ERR_CUDA;
+  const int blocks = nsm * 8;
+  if (sink_len < blocks) return ZL_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (which == 0)
+    xu_probe<<<blocks, 256, 0, st>>>(sink_dev, iters, 1.0f);
+  else
+    fma_probe<<<blocks, 256, 0, st>>>(sink_dev, iters, 1.0f);
+  if (cudaGetLastError() != cudaSuccess) return ZL_ERR_CUDA;
+  *ops_per_launch = (double)blocks * 256.0 * 8.0 * (double)iters;
+  return ZL_OK;
+}

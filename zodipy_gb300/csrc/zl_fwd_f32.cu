@@ -1,0 +1,323 @@
+// Fast forward kernel: the Kelsall integrand in float32 on the FP32/MUFU pipes.
+//
+// Same integral as the float64 kernel (zodipy/model.py:253-277); what changes is
+// the arithmetic, chosen for GB300 where FP64 runs at a small fraction of FP32:
+//  - the cutoff-sphere intersections (zodipy/line_of_sight.py:64-85) are solved
+//    per pixel in float-float (~48-bit) arithmetic;
+//  - for the ring and the feature (zodipy/number_density.py:113-181), whose
+//    radial profiles are narrow (sigma_r = 0.025 AU), node positions and
+//    R^2 - R0^2 are carried in float-float and R - R0 is recovered with one
+//    Newton step, so the Gaussian exponent keeps float32 relative accuracy;
+//  - every other density, T(R) = T0 R^-delta and the table lookup run in
+//    float32, with powers as ex2/lg2 and integer powers by squaring;
+//  - each component's quadrature sum is Kahan-compensated in float32 and
+//    written as float64.
+// One thread integrates one pixel over all nodes and components in node order,
+// so a pixel's result never depends on how pixels are partitioned.
+#include "zl_common.cuh"
+
+namespace zl {
+
+// Compile-time component layouts.  Nibble c: bit0 present, bit1 first component
+// of a new LOS range, bits 2-3 component type.  LAYOUT 0 = generic (runtime).
+constexpr uint32_t kLayoutDirbe = 0xFB5553u;   // cloud | band band band (same range) | ring | feature
+constexpr uint32_t kLayoutPlanck = 0x5553u;    // cloud | band band band
+constexpr uint32_t kLayoutGeneric = 0u;
+
+template <uint32_t LAYOUT>
+struct Lay {
+  static constexpr bool generic = (LAYOUT == 0u);
+  __host__ __device__ static constexpr int ncomp() {
+    if (generic) return ZL_MAX_COMPS;
+    int n = 0;
+    for (int c = 0; c < ZL_MAX_COMPS; ++c)
+      if ((LAYOUT >> (4 * c)) & 1u) n = c + 1;
+    return n;
+  }
+  __host__ __device__ static constexpr int type(int c) { return (int)((LAYOUT >> (4 * c + 2)) & 3u); }
+  __host__ __device__ static constexpr bool first(int c) { return ((LAYOUT >> (4 * c + 1)) & 1u) != 0; }
+};
+
+// Root of |obs + s u| = cutoff (line_of_sight.py:80-85) in float-float; b omits
+// z_obs u_z like the reference.  At b == 0 the root is taken with sign(+0).
+__device__ __forceinline__ ff sphere_distance_ff(ff b, ff r2, ff cut2) {
+  const ff c = ff_add(r2, ff_neg(cut2));
+  const ff D = ff_add(ff_mul(b, b), ff_scale(c, -4.0f));
+  const ff sq = ff_sqrt(D);
+  const ff q = ff_scale(ff_add(b, (b.hi < 0.f || (b.hi == 0.f && signbit(b.hi))) ? ff_neg(sq) : sq), -0.5f);
+  const ff cq = ff_div(c, q);
+  if (isnan(q.hi) || isnan(cq.hi)) return {q.hi + cq.hi, 0.f};
+  return (q.hi > cq.hi || (q.hi == cq.hi && q.lo >= cq.lo)) ? q : cq;
+}
+
+__device__ __forceinline__ float bb_lookup(const float4* __restrict__ tab, float T, float t_min, float t_max,
+                                           float inv_dt, int nT) {
+  const float Tc = fminf(fmaxf(T, t_min), t_max);
+  int j = floor_nonneg((Tc - t_min) * inv_dt);
+  j = min(j, nT - 2);
+  const float4 e = tab[j];  // (T_j, B_j, slope_j, -)
+  return fmaf(e.z, Tc - e.x, e.y);
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float t) {
+  const float y = t - c;
+  const float s1 = s + y;
+  c = (s1 - s) - y;
+  s = s1;
+}
+
+template <int NSPEC, uint32_t LAYOUT, bool PRECISE>
+__global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
+                                                      const double* __restrict__ u, int64_t n_pix,
+                                                      const ZlObserver* __restrict__ observers, int n_obs,
+                                                      double* __restrict__ out_comps, double* __restrict__ out_total) {
+  using L = Lay<LAYOUT>;
+  constexpr int NC = L::ncomp();
+  extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
+  const int nT = P.n_temps;
+  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  __syncthreads();
+
+  const int nc = L::generic ? P.n_comps : NC;
+  const int nr = P.n_ranges;
+
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
+    // ---- per-pixel set-up -------------------------------------------------
+    const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+    const ZlObserver& O = observers[find_observer(observers, n_obs, i)];
+    const ff ox = ff_from_double(O.obs[0]), oy = ff_from_double(O.obs[1]), oz = ff_from_double(O.obs[2]);
+    const uint32_t outside = O.outside;
+    const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
+    const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
+
+    const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+    const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+    const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));  // u . X_obs
+
+    ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
+#pragma unroll
+    for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+      if (r < nr) {
+        const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
+                                                  : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
+        const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
+                                                      : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
+        hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+        mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+      } else {
+        hs_r[r] = ff{0.f, 0.f};
+        mid_r[r] = ff{0.f, 0.f};
+      }
+    }
+
+    // scattering geometry: |u x X_obs| and u . X_obs (scattering.py:26-31 rewritten as atan2)
+    float bperp = 0.f;
+    if (P.has_scat) {
+      const float cx = uyf * ozf - uzf * oyf, cy = uzf * oxf - uxf * ozf, cz = uxf * oyf - uyf * oxf;
+      bperp = sqrtf(cx * cx + cy * cy + cz * cz);
+    }
+
+    // per-component set-up
+    ff hs_c[NC], mid_c[NC], beta_c[NC], gam_c[NC];
+    float un_c[NC], on_c[NC], ocx[NC], ocy[NC], ocz[NC], te_c[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (c >= nc) break;
+      const KCompF32& C = P.comp[c];
+      const int type = L::generic ? C.type : L::type(c);
+      ff hs = {0.f, 0.f}, md = {0.f, 0.f};
+#pragma unroll
+      for (int r = 0; r < ZL_MAX_RANGES; ++r)
+        if (r == C.range) {
+          hs = hs_r[r];
+          md = mid_r[r];
+        }
+      hs_c[c] = hs;
+      mid_c[c] = md;
+      ocx[c] = oxf - C.ox;
+      ocy[c] = oyf - C.oy;
+      ocz[c] = ozf - C.oz;
+      un_c[c] = uxf * C.nx + uyf * C.ny + uzf * C.nz;
+      on_c[c] = ocx[c] * C.nx + ocy[c] * C.ny + ocz[c] * C.nz;
+      beta_c[c] = ff{0.f, 0.f};
+      gam_c[c] = ff{0.f, 0.f};
+      te_c[c] = 0.f;
+      if (PRECISE && (type == ZL_RING || type == ZL_FEATURE)) {
+        if (C.zero_offset) {
+          beta_c[c] = beta_h;
+          gam_c[c] = ff_add(r2, ff_neg(ff{C.c[4], C.c[5]}));
+        } else {
+          const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
+                   dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+          beta_c[c] = ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
+          gam_c[c] = ff_add(ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz)), ff_neg(ff{C.c[4], C.c[5]}));
+        }
+      }
+      if (type == ZL_FEATURE) {
+        te_c[c] = atan2f((float)(O.earth[1] - (double)C.oy), (float)(O.earth[0] - (double)C.ox));
+      }
+    }
+
+    float acc_s[NC][NSPEC], acc_c[NC][NSPEC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) {
+        acc_s[c][s] = 0.f;
+        acc_c[c][s] = 0.f;
+      }
+
+    // ---- quadrature nodes ------------------------------------------------
+#pragma unroll 1
+    for (int k = 0; k < P.n_nodes; ++k) {
+      const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
+      const float wk = P.gl_w[k];
+      float Rl = 0.f, X0 = 0.f, X1 = 0.f, X2 = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
+      float B[NSPEC], sf[NSPEC];
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) {
+        B[s] = 0.f;
+        sf[s] = 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c >= nc) break;
+        const KCompF32& C = P.comp[c];
+        const int type = L::generic ? C.type : L::type(c);
+        const bool first = L::generic ? (C.first_in_range != 0) : L::first(c);
+        const bool precise = PRECISE && (type == ZL_RING || type == ZL_FEATURE);
+        ff Rff = {0.f, 0.f};
+        if (precise) Rff = ff_fma(hs_c[c], xk, mid_c[c]);
+        if (first) {
+          // brightness.py:27-33 — node position, heliocentric distance, temperature
+          Rl = precise ? Rff.hi : fmaf(hs_c[c].hi, xk.hi, mid_c[c].hi);
+          X0 = fmaf(Rl, uxf, oxf);
+          X1 = fmaf(Rl, uyf, oyf);
+          X2 = fmaf(Rl, uzf, ozf);
+          R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
+          rinv = rsqrtf(R2);
+          R = R2 * rinv;
+          lg2R = __log2f(R);
+          const float T = P.T0 * exp2f(P.neg_delta * lg2R);  // blackbody.py:16-30
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) B[s] = bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
+          if (P.has_scat) {  // scattering.py:11-59
+            const float theta = atan2f(bperp, -(Rl + beta_h.hi));
+            const float flux = rinv * rinv;
+#pragma unroll
+            for (int s = 0; s < NSPEC; ++s) {
+              const KSpecF32& S = P.spec[s];
+              sf[s] = S.S * flux * (S.N * (S.C1 + S.C2 * theta + exp2f(S.C3l2e * theta)));
+            }
+          }
+        }
+        // own distance when the component is offset from the Sun
+        float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R, Xc0 = X0, Xc1 = X1;
+        if (!C.zero_offset) {
+          Xc0 = fmaf(Rl, uxf, ocx[c]);
+          Xc1 = fmaf(Rl, uyf, ocy[c]);
+          const float Xc2 = fmaf(Rl, uzf, ocz[c]);
+          Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
+          rcinv = rsqrtf(Rc2);
+          Rc = Rc2 * rcinv;
+          lg2Rc = 0.5f * __log2f(Rc2);
+        }
+        const float Z = fmaf(Rl, un_c[c], on_c[c]);
+        float dens;
+        if (type == ZL_CLOUD) {  // number_density.py:60-73
+          const float zeta = fabsf(Z) * rcinv;
+          const float g = zeta < C.c[4] ? zeta * zeta * C.c[5] : zeta - C.c[6];
+          const float gg = exp2f(C.c[3] * __log2f(g));
+          dens = C.c[0] * exp2f(-C.c[1] * lg2Rc - C.c[2] * gg);
+        } else if (type == ZL_BAND) {  // number_density.py:99-110
+          const float zz = fabsf(Z) * rcinv * C.c[1];
+          const float z2 = zz * zz;
+          const float t2 = exp2f(-kLog2e * (z2 * z2 * z2));
+          const float zp = C.c[5] != 0.f ? z2 * z2 : exp2f(C.c[3] * __log2f(zz));
+          const float t3 = fmaf(zp, C.c[2], 1.0f);
+          const float q = Rc2 * C.c[4];  // (R/delta_r)^2
+          const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+          const float y = q8 * q2;  // (R/delta_r)^20
+          const float t4 = y < 1e-3f ? y * fmaf(-0.5f, y, 1.0f) : 1.0f - exp2f(-kLog2e * y);
+          dens = C.c[0] * rcinv * t2 * t3 * t4;
+        } else {  // ring (number_density.py:136-139) and feature (:167-181)
+          float dR = Rc - C.c[1];
+          if (precise) {
+            // R^2 - R0^2 = R_los (R_los + 2 beta) + gamma, exact to ~2^-48; one Newton step on R
+            const ff t = ff_add(Rff, ff_scale(beta_c[c], 2.0f));
+            const ff D2 = ff_add(ff_mul(Rff, t), gam_c[c]);
+            dR = dR + (D2.hi - dR * (Rc + C.c[1])) * (0.5f * rcinv);
+          }
+          float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
+          if (type == ZL_FEATURE) {
+            float dth = (atan2f(Xc1, Xc0) - te_c[c]) - C.c[6];
+            float d = dth + kPiF;
+            d = d - kTwoPiF * floorf(d * kInvTwoPiF);
+            dth = d - kPiF;
+            arg = fmaf(dth * dth, C.c[7], arg);
+          }
+          dens = C.c[0] * exp2f(-arg);
+        }
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) {
+          const KSpecF32& S = P.spec[s];
+          float e = S.em1[c] * B[s];
+          if (P.has_scat) e = fmaf(S.alb[c], sf[s], e);
+          kahan_add(acc_s[c][s], acc_c[c][s], wk * (e * dens));
+        }
+      }
+    }
+
+    // ---- outputs: x (stop - start)/2, component order total ----------------
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) {
+      double tot = 0.0;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c >= nc) break;
+        const double v = ((double)acc_s[c][s] - (double)acc_c[c][s]) * ((double)hs_c[c].hi + (double)hs_c[c].lo);
+        if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + i] = v;
+        tot = (c == 0) ? v : tot + v;
+      }
+      if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
+    }
+  }
+}
+
+template <int NSPEC, uint32_t LAYOUT, bool PRECISE>
+static cudaError_t launch_f32_t(const KParamsF32& P, const double* u, int64_t n, const ZlObserver* obs, int n_obs,
+                                double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+  const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
+  const int64_t blocks_needed = (n + tpb - 1) / tpb;
+  int64_t grid = (int64_t)num_sms * bps;
+  if (grid > blocks_needed) grid = blocks_needed;
+  if (grid < 1) grid = 1;
+  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, n_obs, oc, ot);
+  return cudaGetLastError();
+}
+
+template <uint32_t LAYOUT>
+static cudaError_t launch_f32_layout(const KParamsF32& P, const double* u, int64_t n, const ZlObserver* obs,
+                                     int n_obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+                                     int num_sms) {
+  switch (P.n_spec) {
+    case 1: return launch_f32_t<1, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+    case 2: return launch_f32_t<2, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+    case 3: return launch_f32_t<3, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+    default: return launch_f32_t<4, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+  }
+}
+
+// layout: 1 = DIRBE-like, 2 = Planck-like, 0 = generic; plain_geometry selects the
+// all-float32 variant of the DIRBE layout (kept for the precision/speed study).
+cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
+                           const ZlObserver* obs, int n_obs, double* oc, double* ot, cudaStream_t st, int tpb,
+                           int bps, int num_sms) {
+  if (layout == 1 && plain_geometry && P.n_spec == 1)
+    return launch_f32_t<1, kLayoutDirbe, false>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+  if (layout == 1) return launch_f32_layout<kLayoutDirbe>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+  if (layout == 2) return launch_f32_layout<kLayoutPlanck>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+  return launch_f32_layout<kLayoutGeneric>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+}
+
+}  // namespace zl

@@ -1,0 +1,85 @@
+"""Device execution: calls into libzodigb on torch CUDA tensors.
+
+PyTorch provides device memory and streams; every kernel that touches pixels
+is libzodigb's own.  There is no CPU path: without a CUDA device or without
+the library these functions raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+PRECISIONS = {"float64": _lib.ZL_PREC_F64, "f64": _lib.ZL_PREC_F64, "float32": _lib.ZL_PREC_F32, "f32": _lib.ZL_PREC_F32}
+
+
+def precision_code(precision) -> int:
+    if isinstance(precision, int) and precision in (_lib.ZL_PREC_F64, _lib.ZL_PREC_F32):
+        return precision
+    try:
+        return PRECISIONS[str(precision).lower()]
+    except KeyError as err:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, got {precision!r}") from err
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise _lib.ZodiGBError("a CUDA device is required: zodipy_gb300 has no CPU evaluation path")
+    return torch
+
+
+def upload_observers(observers, device=None):
+    """Copy a ctypes ``ZlObserver`` array to a uint8 device tensor."""
+    torch = _torch()
+    raw = np.frombuffer(observers, dtype=np.uint8).copy()
+    return torch.from_numpy(raw).to(device or "cuda")
+
+
+def current_stream_handle(device=None) -> int:
+    torch = _torch()
+    return int(torch.cuda.current_stream(device).cuda_stream)
+
+
+def forward(
+    zl_model: _lib.ZlModel,
+    u_dev,
+    observers_dev,
+    n_obs: int,
+    precision,
+    want_comps: bool = True,
+    want_total: bool = True,
+    out_comps=None,
+    out_total=None,
+    stream: int | None = None,
+):
+    """Run ``zl_forward``; returns (comps [n_spec, C, N] or None, total [n_spec, N] or None)."""
+    torch = _torch()
+    if u_dev.dtype != torch.float64 or not u_dev.is_cuda or u_dev.dim() != 2 or u_dev.shape[0] != 3:
+        raise ValueError("unit vectors must be a float64 CUDA tensor of shape (3, N)")
+    u_dev = u_dev.contiguous()
+    n = u_dev.shape[1]
+    ns, nc = zl_model.n_spec, zl_model.n_comps
+    dev = u_dev.device
+    if want_comps and out_comps is None:
+        out_comps = torch.empty((ns, nc, n), dtype=torch.float64, device=dev)
+    if want_total and out_total is None:
+        out_total = torch.empty((ns, n), dtype=torch.float64, device=dev)
+    lib = _lib.load()
+    rc = lib.zl_forward(
+        ctypes.byref(zl_model),
+        ctypes.c_void_p(u_dev.data_ptr()),
+        n,
+        ctypes.c_void_p(observers_dev.data_ptr()),
+        n_obs,
+        precision_code(precision),
+        ctypes.c_void_p(out_comps.data_ptr() if out_comps is not None else 0),
+        ctypes.c_void_p(out_total.data_ptr() if out_total is not None else 0),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(dev)),
+    )
+    _lib.check(rc, "zl_forward")
+    return (out_comps if want_comps else None), (out_total if want_total else None)

@@ -1,0 +1,303 @@
+"""``Model``: the drop-in front end for ZodiPy's ``zodipy.Model``.
+
+Constructor and ``evaluate`` keep the reference's signature, argument meaning,
+validation order and exception types (``zodipy/model.py:36-203``).  Below the
+``_evaluate`` seam (``model.py:205-279``) the line-of-sight integrals run in
+libzodigb's CUDA kernels:
+
+- ``precision="float64"`` (default) runs the plain float64 kernel, which
+  reproduces the reference's numbers to ~1e-15 relative;
+- ``precision="float32"`` runs the float32-bulk kernel (<= 1e-5 relative to
+  float64, typically ~1e-7).
+
+``nprocesses`` is accepted for compatibility; the GPU replaces the fork pool.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+from scipy import integrate
+
+from . import engine, packing
+from .components import ComponentLabel
+from .coords import SkyCoord as _LiteSkyCoord
+from .ephemeris import body_position
+from .spectral import blackbody_table, interp_spectral_param
+from .units import AU, MJy, Quantity, UnitConversionError, as_quantity, sr
+from .zodiacal_light_model import Kelsall, model_registry
+
+
+def _astropy():
+    try:
+        import astropy.coordinates as coords
+        import astropy.units as u
+
+        return coords, u
+    except Exception:  # astropy is optional
+        return None, None
+
+
+class Model:
+    """Zodiacal light model evaluated on the GPU."""
+
+    def __init__(
+        self,
+        x,
+        *,
+        weights=None,
+        name: str = "dirbe",
+        gauss_quad_degree: int = 50,
+        extrapolate: bool = False,
+        ephemeris: str = "builtin",
+        precision: str = "float64",
+    ) -> None:
+        try:
+            if not x.isscalar and weights is None:
+                raise ValueError("Bandpass weights must be provided for non-scalar `x`.")
+        except AttributeError as error:
+            raise TypeError("The input 'x' must be an astropy Quantity.") from error
+        if x.isscalar and weights is not None:
+            raise ValueError("Bandpass weights should not be provided for scalar `x`.")
+        xq = as_quantity(x)
+
+        self._ipd_model = model_registry.get_model(name)
+        if not extrapolate and not self._ipd_model.is_valid_at(xq):
+            raise ValueError(
+                "The requested frequencies are outside the valid range of the model. "
+                "If this was intended, set the extrapolate argument to True."
+            )
+        if weights is not None:
+            weights = np.asarray(weights, dtype=np.float64)
+            if xq.size != weights.size:
+                raise ValueError("Number of wavelengths and weights must be the same in the bandpass.")
+            normalized_weights = weights / integrate.trapezoid(weights, np.asarray(xq.value))
+        else:
+            normalized_weights = None
+
+        self._x = xq
+        self._bounds_error = not extrapolate
+        self._normalized_weights = normalized_weights
+        self._b_nu_table = blackbody_table(xq.value, xq.unit.kind, xq.unit.scale, normalized_weights)
+        self._gauss_quad_degree = int(gauss_quad_degree)
+        self._quad_points, self._quad_weights = np.polynomial.legendre.leggauss(self._gauss_quad_degree)
+        self._ephemeris = ephemeris
+        self._precision = engine.precision_code(precision)
+        self._init_ipd_model_partials()
+
+    # -- set-up -------------------------------------------------------------
+    def _init_ipd_model_partials(self) -> None:
+        """Spectral unpacking (``unpack_model.py:23-107``) and kernel parameter block."""
+        self._interped_comp_params, self._interped_shared_params = self._unpack()
+        spec = {
+            "emissivity": [self._interped_comp_params[k]["emissivity"] for k in self._ipd_model.comps],
+            "albedo": [self._interped_comp_params[k]["albedo"] for k in self._ipd_model.comps],
+            **{k: self._interped_shared_params[k] for k in ("C1", "C2", "C3", "solar_irradiance")},
+        }
+        self._spectrum = spec
+        self._zl_model = packing.pack_model(
+            self._ipd_model, [spec], [self._b_nu_table], self._quad_points, self._quad_weights
+        )
+
+    def _unpack(self):
+        model = self._ipd_model
+        xm = self._x.to_value(model.spectrum.unit, equivalencies="spectral")
+        w = self._normalized_weights
+        spectrum = np.asarray(model.spectrum.value)
+
+        def isp(table, nearest=False):
+            return float(interp_spectral_param(xm, w, spectrum, table, use_nearest=nearest, bounds_error=self._bounds_error))
+
+        comp_params = {}
+        for label in model.comps:
+            comp_params[label] = {
+                "emissivity": isp(model.emissivities[label]),
+                "albedo": isp(model.albedos[label]) if model.albedos is not None else 0.0,
+            }
+        shared = {"T_0": model.T_0, "delta": model.delta}
+        for key in ("C1", "C2", "C3"):
+            table = getattr(model, key)
+            shared[key] = isp(table, nearest=True) if table is not None else 0.0
+        shared["solar_irradiance"] = isp(model.solar_irradiance) if model.solar_irradiance is not None else 0.0
+        return comp_params, shared
+
+    # -- public API -----------------------------------------------------------
+    def evaluate(self, skycoord, *, obspos="earth", return_comps: bool = False, nprocesses: int = 1):
+        """Zodiacal emission [MJy/sr] toward every coordinate (``model.py:119-203``)."""
+        try:
+            if skycoord.obstime is None:
+                raise ValueError("The `obstime` attribute of the `SkyCoord` object is not set.")
+        except AttributeError as error:
+            raise TypeError("The input coordinates must be an astropy SkyCoord object.") from error
+        obstime_mjd = np.asarray(skycoord.obstime.mjd, dtype=np.float64)
+        n_time = obstime_mjd.size
+        try:
+            if not (obspos_isstr := isinstance(obspos, str)) and (
+                (obspos.ndim > 1 and n_time != obspos.shape[-1]) or (obspos.ndim == 1 and n_time != 1)
+            ):
+                raise ValueError("The number of obstime (ncoords) and obspos (3, ncoords) does not match.")
+        except AttributeError as error:
+            raise TypeError("The observer position is not a string or an astropy Quantity.") from error
+        if n_time > skycoord.size:
+            raise ValueError("The size of obstime must be either 1 or ncoords.")
+
+        earth_xyz = self._earth_position(obstime_mjd)
+        if obspos_isstr:
+            obs_xyz = self._body_position(obspos, obstime_mjd, earth_xyz)
+        else:
+            try:
+                obs_xyz = as_quantity(obspos).to_value(AU)
+            except UnitConversionError as error:
+                raise UnitConversionError("The observer position must be in length units.") from error
+        unit_vectors = self._unit_vectors(skycoord)
+        emission = self._evaluate(unit_vectors, np.asarray(obs_xyz, dtype=np.float64), earth_xyz, return_comps)
+        return self._as_output_quantity(emission, skycoord)
+
+    def evaluate_xyz(self, unit_vectors, obs_pos, earth_pos=None, *, return_comps: bool = False, precision=None, out=None):
+        """The ``_evaluate`` seam on explicit heliocentric-ecliptic vectors.
+
+        ``unit_vectors``: (3, N) float64 — a numpy array, a (preferably pinned)
+        CPU tensor, or a CUDA tensor; ``obs_pos`` / ``earth_pos``: (3,) or
+        (3, N) in AU.  Returns float64 (C, N) or (N,): a numpy array for host
+        input, a CUDA tensor for device input.  ``out`` (host input only) is a
+        pinned CPU tensor of the result's shape to receive it.
+        """
+        if earth_pos is None:
+            earth_pos = np.asarray(obs_pos, dtype=np.float64)
+        return self._evaluate(unit_vectors, obs_pos, earth_pos, return_comps, precision, out)
+
+    def get_parameters(self) -> dict:
+        return self._ipd_model.to_dict()
+
+    def update_parameters(self, parameters: dict) -> None:
+        """Rebuild the model from a ``get_parameters()`` dict (``model.py:311-333``)."""
+        d = parameters.copy()
+        d["comps"] = {}
+        for key, value in parameters.items():
+            if key == "comps":
+                for comp_key, comp_value in value.items():
+                    label = ComponentLabel(comp_key)
+                    d["comps"][label] = type(self._ipd_model.comps[label])(**comp_value)
+            elif isinstance(value, dict):
+                d[key] = {ComponentLabel(k): v for k, v in value.items()}
+        self._ipd_model = self._ipd_model.__class__(**d)
+        self._init_ipd_model_partials()
+
+    @property
+    def ncomps(self) -> int:
+        return self._ipd_model.ncomps
+
+    @property
+    def comp_labels(self) -> list[str]:
+        return [k.value for k in self._ipd_model.comps]
+
+    @property
+    def zl_model(self):
+        """The packed C-ABI model description (``ZlModel``)."""
+        return self._zl_model
+
+    @property
+    def precision(self) -> int:
+        return self._precision
+
+    # -- internals -----------------------------------------------------------
+    def _earth_position(self, mjd: np.ndarray) -> np.ndarray:
+        coords, u = _astropy()
+        if coords is not None:
+            from astropy.time import Time
+
+            t = Time(mjd, format="mjd")
+            pos = coords.get_body("earth", t, ephemeris=self._ephemeris).transform_to(coords.HeliocentricMeanEcliptic)
+            return np.asarray(pos.cartesian.xyz.to_value(u.AU), dtype=np.float64).reshape(3, -1)
+        return body_position("earth", mjd).reshape(3, -1)
+
+    def _body_position(self, body: str, mjd: np.ndarray, earth_xyz: np.ndarray) -> np.ndarray:
+        body = body.lower()
+        if body == "earth":
+            return earth_xyz
+        if body == "semb-l2":
+            from .ephemeris import semb_l2
+
+            return semb_l2(earth_xyz)
+        coords, u = _astropy()
+        if coords is not None:
+            from astropy.time import Time
+
+            try:
+                pos = coords.get_body(body, Time(mjd, format="mjd"), ephemeris=self._ephemeris)
+            except KeyError as error:
+                raise ValueError(f"Invalid observer string: '{body}'.") from error
+            pos = pos.transform_to(coords.HeliocentricMeanEcliptic)
+            return np.asarray(pos.cartesian.xyz.to_value(u.AU), dtype=np.float64).reshape(3, -1)
+        return body_position(body, mjd).reshape(3, -1)
+
+    @staticmethod
+    def _unit_vectors(skycoord) -> np.ndarray:
+        if isinstance(skycoord, _LiteSkyCoord):
+            return skycoord.ecliptic_unit_vectors()
+        coords, _ = _astropy()
+        if coords is None:
+            raise TypeError("The input coordinates must be an astropy SkyCoord object.")
+        sc = skycoord.transform_to(coords.BarycentricMeanEcliptic)
+        xyz = np.asarray(sc.cartesian.xyz.value, dtype=np.float64)
+        return xyz.reshape(3, -1)
+
+    @staticmethod
+    def _as_output_quantity(emission, skycoord):
+        if isinstance(skycoord, _LiteSkyCoord):
+            return Quantity(emission, MJy / sr)
+        _, u = _astropy()
+        return emission << (u.MJy / u.sr)
+
+    def _evaluate(self, unit_vectors, obs_xyz, earth_xyz, return_comps, precision=None, out=None):
+        import torch
+
+        prec = self._precision if precision is None else engine.precision_code(precision)
+        on_device = isinstance(unit_vectors, torch.Tensor) and unit_vectors.is_cuda
+        n = unit_vectors.shape[-1]
+        obs = np.asarray(obs_xyz.detach().cpu() if isinstance(obs_xyz, torch.Tensor) else obs_xyz, dtype=np.float64)
+        earth = np.asarray(
+            earth_xyz.detach().cpu() if isinstance(earth_xyz, torch.Tensor) else earth_xyz, dtype=np.float64
+        )
+        obs = obs.reshape(3, -1)
+        earth = earth.reshape(3, -1)
+        if obs.shape[1] not in (1, n) or earth.shape[1] not in (1, n):
+            raise ValueError("positions must be (3,) or (3, ncoords)")
+        per_pixel = obs.shape[1] > 1 or earth.shape[1] > 1
+        if per_pixel:
+            # time-ordered input: one observer record per pixel, cutoff flags OR-ed
+            # over the call (line_of_sight.py:72 tests `.any()` over all positions)
+            n_rec = n
+            obs = np.broadcast_to(obs, (3, n))
+            earth = np.broadcast_to(earth, (3, n))
+            pix_begin = np.arange(n, dtype=np.int64)
+        else:
+            n_rec = 1
+            pix_begin = np.zeros(1, dtype=np.int64)
+        table = packing.observer_table(self._zl_model, obs, earth, pix_begin, any_mode=per_pixel)
+        obs_dev = engine.upload_observers(table)
+        if on_device:
+            u_dev = unit_vectors.to(torch.float64).contiguous()
+        else:
+            if isinstance(unit_vectors, torch.Tensor):
+                u_host = unit_vectors.to(torch.float64).reshape(3, n).contiguous()
+            else:
+                u_host = torch.from_numpy(np.ascontiguousarray(np.asarray(unit_vectors, dtype=np.float64).reshape(3, n)))
+            if not u_host.is_pinned():
+                u_host = u_host.pin_memory()
+            u_dev = u_host.to("cuda", non_blocking=True)
+        comps, total = engine.forward(self._zl_model, u_dev, obs_dev, n_rec, prec, return_comps, not return_comps)
+        res = comps[0] if return_comps else total[0]
+        if on_device:
+            return res
+        if out is None:
+            host = torch.empty(res.shape, dtype=torch.float64, pin_memory=True)
+        else:
+            if not isinstance(out, torch.Tensor) or tuple(out.shape) != tuple(res.shape) or out.dtype != torch.float64:
+                raise ValueError(f"out must be a float64 CPU tensor of shape {tuple(res.shape)}")
+            host = out
+        host.copy_(res, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return host if out is not None else host.numpy()
+
+
+__all__ = ["Model", "Kelsall"]
