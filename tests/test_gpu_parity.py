@@ -1,9 +1,12 @@
 """GPU parity: libzodigb's kernels against the reference's golden outputs and the oracle.
 
-Tolerances (relative):
-  float64 plain kernel vs reference/oracle ........ 1e-10 per component
-  float32-bulk kernel vs float64 ................... 1e-5 on the total, and per
-      component 1e-5 relative to max(|component|, 1e-3 |total|)
+Tolerances:
+  float64 plain kernel vs reference/oracle ........ 1e-10 relative per component,
+      with an absolute floor of 1e-200 MJy/sr: single quadrature terms below
+      ~1e-300 are subnormal and keep only a few bits, so relative comparison
+      means nothing there (e.g. a dust band 3 widths off its plane, e^-729)
+  float32-bulk kernel vs float64 ................... 1e-5 relative on the total, and
+      per component 1e-5 relative to max(|component|, 1e-3 |total|)
 """
 
 import numpy as np
@@ -15,7 +18,18 @@ from oracle import zodi_oracle as zo
 pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not cuda_ok(), reason="needs CUDA")]
 
 F64_RTOL = 1e-10
+F64_ATOL = 1e-200
 F32_RTOL = 1e-5
+
+
+def assert_f64_close(got, ref, what=""):
+    err = np.abs(got - ref) - F64_RTOL * np.abs(ref)
+    bad = err > F64_ATOL
+    if bad.any():
+        c, i = np.unravel_index(np.argmax(np.where(bad, np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300), 0)), got.shape)
+        raise AssertionError(
+            f"{what}: {bad.sum()} elements off; worst comp {c} pixel {i}: got {got[c, i]!r} ref {ref[c, i]!r}"
+        )
 
 
 def _ref_fixed(case):
@@ -47,9 +61,7 @@ def test_f64_matches_reference(lib, name):
     ref = _ref_fixed(case)
     assert got.shape == ref.shape
     assert np.isfinite(got).all()
-    nz = ref != 0
-    np.testing.assert_array_equal(got[~nz], 0.0)
-    np.testing.assert_allclose(got[nz], ref[nz], rtol=F64_RTOL, atol=0)
+    assert_f64_close(got, ref, name)
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -59,8 +71,12 @@ def test_f32_matches_reference(lib, name):
     got = _eval(model, case, "float32")
     ref = _ref_fixed(case)
     e_tot, e_comp = rel_err_f32(got, ref)
-    assert e_tot.max() <= F32_RTOL, f"total max rel err {e_tot.max():.3e}"
-    assert e_comp.max() <= F32_RTOL, f"component max rel err {e_comp.max():.3e}"
+    c, i = np.unravel_index(np.argmax(e_comp), e_comp.shape)
+    assert e_tot.max() <= F32_RTOL, f"total max rel err {e_tot.max():.3e} at pixel {np.argmax(e_tot)}"
+    assert e_comp.max() <= F32_RTOL, (
+        f"component max rel err {e_comp.max():.3e}: comp {c} pixel {i} got {got[c, i]!r} ref {ref[c, i]!r} "
+        f"total {ref[:, i].sum()!r}"
+    )
 
 
 @pytest.mark.parametrize("precision", ["float64", "float32"])
@@ -101,9 +117,9 @@ def test_f64_vs_oracle_random_observers(lib):
         earth = np.array([np.cos(rng.uniform(0, 6.28)), np.sin(rng.uniform(0, 6.28)), 0.0])
         ref = zo.evaluate(desc, v, obs, earth, fix_b0=True)
         got = model.evaluate_xyz(v, obs, earth, return_comps=True, precision="float64")
-        nz = ref != 0
-        np.testing.assert_array_equal(got[~nz], 0.0)
-        np.testing.assert_allclose(got[nz], ref[nz], rtol=F64_RTOL)
+        assert_f64_close(got, ref, "random observer")
+        e_tot, e_comp = rel_err_f32(model.evaluate_xyz(v, obs, earth, return_comps=True, precision="float32"), ref)
+        assert e_tot.max() <= F32_RTOL and e_comp.max() <= F32_RTOL
 
 
 def test_empty_and_single(lib):
@@ -112,7 +128,7 @@ def test_empty_and_single(lib):
     out = model.evaluate_xyz(np.zeros((3, 0)), case["obs"], case["earth"], return_comps=True)
     assert out.shape == (6, 0)
     one = model.evaluate_xyz(case["unit_vectors"], case["obs"], case["earth"], return_comps=True)
-    np.testing.assert_allclose(one, case["ref_out"], rtol=F64_RTOL)
+    assert_f64_close(one, case["ref_out"], "single")
 
 
 def test_device_tensors_stay_on_device(lib):

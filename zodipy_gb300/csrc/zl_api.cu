@@ -141,14 +141,17 @@ int detect_layout(const ZlModel& m) {
   first_in_range(m, first);
   static const int dirbe_t[6] = {ZL_CLOUD, ZL_BAND, ZL_BAND, ZL_BAND, ZL_RING, ZL_FEATURE};
   static const int dirbe_f[6] = {1, 0, 0, 0, 1, 1};
+  static const int dirbe_r[6] = {0, 0, 0, 0, 1, 2};
   if (m.n_comps == 6) {
     bool ok = true;
-    for (int c = 0; c < 6; ++c) ok = ok && m.comp[c].type == dirbe_t[c] && first[c] == dirbe_f[c];
+    for (int c = 0; c < 6; ++c)
+      ok = ok && m.comp[c].type == dirbe_t[c] && first[c] == dirbe_f[c] && m.comp[c].range == dirbe_r[c];
     if (ok) return 1;
   }
   if (m.n_comps == 4) {
     bool ok = true;
-    for (int c = 0; c < 4; ++c) ok = ok && m.comp[c].type == dirbe_t[c] && first[c] == dirbe_f[c];
+    for (int c = 0; c < 4; ++c)
+      ok = ok && m.comp[c].type == dirbe_t[c] && first[c] == dirbe_f[c] && m.comp[c].range == dirbe_r[c];
     if (ok) return 2;
   }
   return 0;
@@ -203,9 +206,9 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
     K.range = C.range;
     K.first_in_range = first[c];
     K.zero_offset = (C.offset[0] == 0.0 && C.offset[1] == 0.0 && C.offset[2] == 0.0) ? 1 : 0;
-    K.nx = (float)(C.sin_Omega * C.sin_i);
-    K.ny = (float)(-C.cos_Omega * C.sin_i);
-    K.nz = (float)C.cos_i;
+    split(C.sin_Omega * C.sin_i, &K.nx, &K.nx_lo);
+    split(-C.cos_Omega * C.sin_i, &K.ny, &K.ny_lo);
+    split(C.cos_i, &K.nz, &K.nz_lo);
     split(C.offset[0], &K.ox, &K.ox_lo);
     split(C.offset[1], &K.oy, &K.oy_lo);
     split(C.offset[2], &K.oz, &K.oz_lo);

@@ -39,6 +39,7 @@ struct KParamsF64 {
 struct KCompF32 {
   int32_t type, range, first_in_range, zero_offset;
   float nx, ny, nz;        // unit normal of the symmetry plane (sinO sini, -cosO sini, cosi)
+  float nx_lo, ny_lo, nz_lo;  // low parts of the normal for float-float heights
   float ox, oy, oz;        // offset X_0 [AU]
   float ox_lo, oy_lo, oz_lo;  // low parts of X_0 for float-float geometry
   // type constants:

@@ -36,6 +36,13 @@ struct Lay {
   }
   __host__ __device__ static constexpr int type(int c) { return (int)((LAYOUT >> (4 * c + 2)) & 3u); }
   __host__ __device__ static constexpr bool first(int c) { return ((LAYOUT >> (4 * c + 1)) & 1u) != 0; }
+  // LOS-range index of component c: ranges are numbered in order of first use
+  __host__ __device__ static constexpr int range(int c) {
+    int r = -1;
+    for (int j = 0; j <= c; ++j)
+      if (first(j)) ++r;
+    return r;
+  }
 };
 
 // Root of |obs + s u| = cutoff (line_of_sight.py:80-85) in float-float; b omits
@@ -126,19 +133,31 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       const KCompF32& C = P.comp[c];
       const int type = L::generic ? C.type : L::type(c);
       ff hs = {0.f, 0.f}, md = {0.f, 0.f};
+      if (!L::generic) {
+        hs = hs_r[L::range(c)];
+        md = mid_r[L::range(c)];
+      } else {
 #pragma unroll
-      for (int r = 0; r < ZL_MAX_RANGES; ++r)
-        if (r == C.range) {
-          hs = hs_r[r];
-          md = mid_r[r];
-        }
+        for (int r = 0; r < ZL_MAX_RANGES; ++r)
+          if (r == C.range) {
+            hs = hs_r[r];
+            md = mid_r[r];
+          }
+      }
       hs_c[c] = hs;
       mid_c[c] = md;
-      ocx[c] = oxf - C.ox;
-      ocy[c] = oyf - C.oy;
-      ocz[c] = ozf - C.oz;
-      un_c[c] = uxf * C.nx + uyf * C.ny + uzf * C.nz;
-      on_c[c] = ocx[c] * C.nx + ocy[c] * C.ny + ocz[c] * C.nz;
+      // heights above the symmetry plane: Z(R_los) = R_los (u . n) + (X_obs - X_0) . n, both
+      // dot products in float-float so that Z keeps float32 relative accuracy near the plane
+      const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
+               dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
+      const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+      ocx[c] = dx.hi + dx.lo;
+      ocy[c] = dy.hi + dy.lo;
+      ocz[c] = dz.hi + dz.lo;
+      un_c[c] = un.hi + un.lo;
+      on_c[c] = on.hi + on.lo;
       beta_c[c] = ff{0.f, 0.f};
       gam_c[c] = ff{0.f, 0.f};
       te_c[c] = 0.f;
@@ -147,8 +166,6 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           beta_c[c] = beta_h;
           gam_c[c] = ff_add(r2, ff_neg(ff{C.c[4], C.c[5]}));
         } else {
-          const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
-                   dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
           beta_c[c] = ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
           gam_c[c] = ff_add(ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz)), ff_neg(ff{C.c[4], C.c[5]}));
         }
@@ -238,7 +255,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           const float q = Rc2 * C.c[4];  // (R/delta_r)^2
           const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
           const float y = q8 * q2;  // (R/delta_r)^20
-          const float t4 = y < 1e-3f ? y * fmaf(-0.5f, y, 1.0f) : 1.0f - exp2f(-kLog2e * y);
+          // 1 - e^-y; below 1/4 by its series (relative error < 1e-7) instead of a cancelling difference
+          const float t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
+                                     : 1.0f - exp2f(-kLog2e * y);
           dens = C.c[0] * rcinv * t2 * t3 * t4;
         } else {  // ring (number_density.py:136-139) and feature (:167-181)
           float dR = Rc - C.c[1];
@@ -275,9 +294,11 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         if (c >= nc) break;
-        const double v = ((double)acc_s[c][s] - (double)acc_c[c][s]) * ((double)hs_c[c].hi + (double)hs_c[c].lo);
+        // explicit roundings: the total must equal the sum of the stored components bit for bit
+        const double v = __dmul_rn(__dsub_rn((double)acc_s[c][s], (double)acc_c[c][s]),
+                                   __dadd_rn((double)hs_c[c].hi, (double)hs_c[c].lo));
         if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + i] = v;
-        tot = (c == 0) ? v : tot + v;
+        tot = (c == 0) ? v : __dadd_rn(tot, v);
       }
       if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
     }
