@@ -206,6 +206,16 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
     K.range = C.range;
     K.first_in_range = first[c];
     K.zero_offset = (C.offset[0] == 0.0 && C.offset[1] == 0.0 && C.offset[2] == 0.0) ? 1 : 0;
+    K.share_t4 = -1;
+    if (C.type == ZL_BAND)
+      for (int j = 0; j < c; ++j) {
+        const ZlComponent& Cj = m.comp[j];
+        if (Cj.type == ZL_BAND && Cj.range == C.range && Cj.p[3] == C.p[3] && Cj.offset[0] == C.offset[0] &&
+            Cj.offset[1] == C.offset[1] && Cj.offset[2] == C.offset[2]) {
+          K.share_t4 = j;
+          break;
+        }
+      }
     split(C.sin_Omega * C.sin_i, &K.nx, &K.nx_lo);
     split(-C.cos_Omega * C.sin_i, &K.ny, &K.ny_lo);
     split(C.cos_i, &K.nz, &K.nz_lo);

@@ -38,6 +38,8 @@ struct KParamsF64 {
 // Per-component constants of the float32 kernel (Kelsall-98 densities).
 struct KCompF32 {
   int32_t type, range, first_in_range, zero_offset;
+  int32_t share_t4;  // band: index of an earlier band with the same delta_r (reuse its 1 - e^-y), else -1
+  int32_t pad_i[3];
   float nx, ny, nz;        // unit normal of the symmetry plane (sinO sini, -cosO sini, cosi)
   float nx_lo, ny_lo, nz_lo;  // low parts of the normal for float-float heights
   float ox, oy, oz;        // offset X_0 [AU]
@@ -120,6 +122,14 @@ __device__ __forceinline__ ff ff_mulf(ff a, float b) {
   return ff_quick(p, e);
 }
 
+// Faster sum: exact TwoSum of the high parts, low parts added once.  Its error is
+// a few units of 2^-48 of the larger operand even under cancellation, which is
+// what the callers need (an absolute accuracy, not a relative one).
+__device__ __forceinline__ ff ff_add_fast(ff a, ff b) {
+  ff s = ff_two_sum(a.hi, b.hi);
+  return ff_quick(s.hi, s.lo + (a.lo + b.lo));
+}
+
 // a * b + c, all float-float
 __device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
 
@@ -149,6 +159,24 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
   ff p = ff_mulf(b, q);
   ff r = ff_add(a, ff_neg(p));
   return ff_quick(q, r.hi / b.hi);
+}
+
+// Single MUFU instructions (flush-to-zero): the integrands never need subnormal
+// results, so the range fix-ups that exp2f/__log2f/rsqrtf wrap around them are skipped.
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float lg2_ftz(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
 // floor of a non-negative float below 2^22 without the conversion pipe

@@ -5,11 +5,15 @@
 //  - the cutoff-sphere intersections (zodipy/line_of_sight.py:64-85) are solved
 //    per pixel in float-float (~48-bit) arithmetic;
 //  - for the ring and the feature (zodipy/number_density.py:113-181), whose
-//    radial profiles are narrow (sigma_r = 0.025 AU), node positions and
-//    R^2 - R0^2 are carried in float-float and R - R0 is recovered with one
-//    Newton step, so the Gaussian exponent keeps float32 relative accuracy;
-//  - every other density, T(R) = T0 R^-delta and the table lookup run in
-//    float32, with powers as ex2/lg2 and integer powers by squaring;
+//    radial profiles are narrow (sigma_r = 0.025 AU), R^2 - R0^2 at each node is
+//    a float-float quadratic in the node abscissa with per-pixel coefficients,
+//    and R - R0 is recovered from it with one Newton step, so the Gaussian
+//    exponent keeps float32 relative accuracy;
+//  - heights above each symmetry plane are linear in the node position with
+//    float-float per-pixel coefficients;
+//  - everything else runs in float32 with single MUFU instructions (ex2, lg2,
+//    rsqrt), integer powers by squaring and 1 - e^-y by its series where it
+//    would cancel;
 //  - each component's quadrature sum is Kahan-compensated in float32 and
 //    written as float64.
 // One thread integrates one pixel over all nodes and components in node order,
@@ -73,6 +77,12 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float t) {
   s = s1;
 }
 
+// float32 value of hs * x + mid from float-float parts, within ~1 ulp
+__device__ __forceinline__ float node_position(ff hs, ff x, ff mid) {
+  const float r = fmaf(hs.hi, x.hi, mid.hi);
+  return r + fmaf(hs.hi, x.lo, fmaf(hs.lo, x.hi, mid.lo));
+}
+
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE>
 __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                       const double* __restrict__ u, int64_t n_pix,
@@ -125,8 +135,8 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
     }
 
     // per-component set-up
-    ff hs_c[NC], mid_c[NC], beta_c[NC], gam_c[NC];
-    float un_c[NC], on_c[NC], ocx[NC], ocy[NC], ocz[NC], te_c[NC];
+    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], a2_c[NC], a1_c[NC], a0_c[NC];
+    float ocx[NC], ocy[NC], ocz[NC], rux[NC], ruy[NC], rox[NC], roy[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       if (c >= nc) break;
@@ -146,32 +156,40 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       }
       hs_c[c] = hs;
       mid_c[c] = md;
-      // heights above the symmetry plane: Z(R_los) = R_los (u . n) + (X_obs - X_0) . n, both
-      // dot products in float-float so that Z keeps float32 relative accuracy near the plane
       const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
                dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
-      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
-      const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
-      const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
       ocx[c] = dx.hi + dx.lo;
       ocy[c] = dy.hi + dy.lo;
       ocz[c] = dz.hi + dz.lo;
-      un_c[c] = un.hi + un.lo;
-      on_c[c] = on.hi + on.lo;
-      beta_c[c] = ff{0.f, 0.f};
-      gam_c[c] = ff{0.f, 0.f};
-      te_c[c] = 0.f;
+      // height above the symmetry plane, linear in the node abscissa x:
+      //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
+      const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+      z1_c[c] = ff_mul(hs, un);
+      z0_c[c] = ff_add(ff_mul(md, un), on);
+      a2_c[c] = a1_c[c] = a0_c[c] = ff{0.f, 0.f};
+      rux[c] = ruy[c] = rox[c] = roy[c] = 0.f;
       if (PRECISE && (type == ZL_RING || type == ZL_FEATURE)) {
-        if (C.zero_offset) {
-          beta_c[c] = beta_h;
-          gam_c[c] = ff_add(r2, ff_neg(ff{C.c[4], C.c[5]}));
-        } else {
-          beta_c[c] = ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
-          gam_c[c] = ff_add(ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz)), ff_neg(ff{C.c[4], C.c[5]}));
-        }
+        // R^2 - R0^2 = a2 x^2 + a1 x + a0 with R_los = hs x + mid,
+        // beta = u . (X_obs - X_0), gamma = |X_obs - X_0|^2 - R0^2
+        const ff beta = C.zero_offset ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
+        const ff d2 = C.zero_offset ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+        const ff gamma = ff_add(d2, ff_neg(ff{C.c[4], C.c[5]}));
+        a2_c[c] = ff_mul(hs, hs);
+        a1_c[c] = ff_scale(ff_mul(hs, ff_add(md, beta)), 2.0f);
+        a0_c[c] = ff_add(ff_mul(md, ff_add(md, ff_scale(beta, 2.0f))), gamma);
       }
       if (type == ZL_FEATURE) {
-        te_c[c] = atan2f((float)(O.earth[1] - (double)C.oy), (float)(O.earth[0] - (double)C.ox));
+        // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
+        // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2
+        const float phi = atan2f((float)(O.earth[1] - (double)C.oy), (float)(O.earth[0] - (double)C.ox)) + C.c[6];
+        float sp, cp;
+        sincosf(phi, &sp, &cp);
+        rux[c] = cp * uxf + sp * uyf;
+        ruy[c] = cp * uyf - sp * uxf;
+        rox[c] = cp * ocx[c] + sp * ocy[c];
+        roy[c] = cp * ocy[c] - sp * ocx[c];
       }
     }
 
@@ -190,7 +208,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
       const float wk = P.gl_w[k];
       float Rl = 0.f, X0 = 0.f, X1 = 0.f, X2 = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
-      float B[NSPEC], sf[NSPEC];
+      float B[NSPEC], sf[NSPEC], t4s[NC];
 #pragma unroll
       for (int s = 0; s < NSPEC; ++s) {
         B[s] = 0.f;
@@ -198,24 +216,24 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       }
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
+        t4s[c] = 0.f;
         if (c >= nc) break;
         const KCompF32& C = P.comp[c];
         const int type = L::generic ? C.type : L::type(c);
         const bool first = L::generic ? (C.first_in_range != 0) : L::first(c);
         const bool precise = PRECISE && (type == ZL_RING || type == ZL_FEATURE);
-        ff Rff = {0.f, 0.f};
-        if (precise) Rff = ff_fma(hs_c[c], xk, mid_c[c]);
         if (first) {
           // brightness.py:27-33 — node position, heliocentric distance, temperature
-          Rl = precise ? Rff.hi : fmaf(hs_c[c].hi, xk.hi, mid_c[c].hi);
+          Rl = node_position(hs_c[c], xk, mid_c[c]);
           X0 = fmaf(Rl, uxf, oxf);
           X1 = fmaf(Rl, uyf, oyf);
           X2 = fmaf(Rl, uzf, ozf);
           R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
-          rinv = rsqrtf(R2);
+          rinv = rsqrt_ftz(R2);
+          rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);  // one Newton step
           R = R2 * rinv;
-          lg2R = __log2f(R);
-          const float T = P.T0 * exp2f(P.neg_delta * lg2R);  // blackbody.py:16-30
+          lg2R = lg2_ftz(R);
+          const float T = P.T0 * ex2_ftz(P.neg_delta * lg2R);  // blackbody.py:16-30
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) B[s] = bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
           if (P.has_scat) {  // scattering.py:11-59
@@ -224,58 +242,67 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 #pragma unroll
             for (int s = 0; s < NSPEC; ++s) {
               const KSpecF32& S = P.spec[s];
-              sf[s] = S.S * flux * (S.N * (S.C1 + S.C2 * theta + exp2f(S.C3l2e * theta)));
+              sf[s] = S.S * flux * (S.N * (S.C1 + S.C2 * theta + ex2_ftz(S.C3l2e * theta)));
             }
           }
         }
         // own distance when the component is offset from the Sun
-        float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R, Xc0 = X0, Xc1 = X1;
+        float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R;
         if (!C.zero_offset) {
-          Xc0 = fmaf(Rl, uxf, ocx[c]);
-          Xc1 = fmaf(Rl, uyf, ocy[c]);
+          const float Xc0 = fmaf(Rl, uxf, ocx[c]);
+          const float Xc1 = fmaf(Rl, uyf, ocy[c]);
           const float Xc2 = fmaf(Rl, uzf, ocz[c]);
           Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
-          rcinv = rsqrtf(Rc2);
+          rcinv = rsqrt_ftz(Rc2);
+          rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
           Rc = Rc2 * rcinv;
-          lg2Rc = 0.5f * __log2f(Rc2);
+          lg2Rc = 0.5f * lg2_ftz(Rc2);
         }
-        const float Z = fmaf(Rl, un_c[c], on_c[c]);
+        const ff Zff = ff_add_fast(ff_mul(z1_c[c], xk), z0_c[c]);
+        const float Z = Zff.hi + Zff.lo;
         float dens;
         if (type == ZL_CLOUD) {  // number_density.py:60-73
           const float zeta = fabsf(Z) * rcinv;
           const float g = zeta < C.c[4] ? zeta * zeta * C.c[5] : zeta - C.c[6];
-          const float gg = exp2f(C.c[3] * __log2f(g));
-          dens = C.c[0] * exp2f(-C.c[1] * lg2Rc - C.c[2] * gg);
+          const float gg = ex2_ftz(C.c[3] * lg2_ftz(g));
+          dens = C.c[0] * ex2_ftz(-C.c[1] * lg2Rc - C.c[2] * gg);
         } else if (type == ZL_BAND) {  // number_density.py:99-110
           const float zz = fabsf(Z) * rcinv * C.c[1];
           const float z2 = zz * zz;
-          const float t2 = exp2f(-kLog2e * (z2 * z2 * z2));
-          const float zp = C.c[5] != 0.f ? z2 * z2 : exp2f(C.c[3] * __log2f(zz));
+          const float t2 = ex2_ftz(-kLog2e * (z2 * z2 * z2));
+          const float zp = C.c[5] != 0.f ? z2 * z2 : ex2_ftz(C.c[3] * lg2_ftz(zz));
           const float t3 = fmaf(zp, C.c[2], 1.0f);
-          const float q = Rc2 * C.c[4];  // (R/delta_r)^2
-          const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
-          const float y = q8 * q2;  // (R/delta_r)^20
-          // 1 - e^-y; below 1/4 by its series (relative error < 1e-7) instead of a cancelling difference
-          const float t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
-                                     : 1.0f - exp2f(-kLog2e * y);
+          float t4 = 0.f;
+          bool shared = false;
+#pragma unroll
+          for (int j = 0; j < NC; ++j)
+            if (j < c && C.share_t4 == j) {
+              t4 = t4s[j];
+              shared = true;
+            }
+          if (!shared) {
+            const float q = Rc2 * C.c[4];  // (R/delta_r)^2
+            const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+            const float y = q8 * q2;  // (R/delta_r)^20
+            // 1 - e^-y; below 1/4 by its series (relative error < 1e-7) instead of a cancelling difference
+            t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
+                           : 1.0f - ex2_ftz(-kLog2e * y);
+          }
+          t4s[c] = t4;
           dens = C.c[0] * rcinv * t2 * t3 * t4;
         } else {  // ring (number_density.py:136-139) and feature (:167-181)
           float dR = Rc - C.c[1];
           if (precise) {
-            // R^2 - R0^2 = R_los (R_los + 2 beta) + gamma, exact to ~2^-48; one Newton step on R
-            const ff t = ff_add(Rff, ff_scale(beta_c[c], 2.0f));
-            const ff D2 = ff_add(ff_mul(Rff, t), gam_c[c]);
+            // R^2 - R0^2 from the float-float quadratic; one Newton step on R
+            const ff D2 = ff_add_fast(ff_mul(ff_add_fast(ff_mul(a2_c[c], xk), a1_c[c]), xk), a0_c[c]);
             dR = dR + (D2.hi - dR * (Rc + C.c[1])) * (0.5f * rcinv);
           }
           float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
           if (type == ZL_FEATURE) {
-            float dth = (atan2f(Xc1, Xc0) - te_c[c]) - C.c[6];
-            float d = dth + kPiF;
-            d = d - kTwoPiF * floorf(d * kInvTwoPiF);
-            dth = d - kPiF;
+            const float dth = atan2f(fmaf(Rl, ruy[c], roy[c]), fmaf(Rl, rux[c], rox[c]));
             arg = fmaf(dth * dth, C.c[7], arg);
           }
-          dens = C.c[0] * exp2f(-arg);
+          dens = C.c[0] * ex2_ftz(-arg);
         }
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
