@@ -307,6 +307,36 @@ def main():
         "component_max": [float(v) for v in e_comp],
     }
 
+    # ---- forward + adjoint (per-pixel loss gradient w.r.t. every parameter) ---
+    g_up = torch.randn((1, n), dtype=torch.float64, device=dev, generator=torch.Generator(dev).manual_seed(7))
+    grad = torch.empty(engine.grad_count(zl), dtype=torch.float64, device=dev)
+    ws = torch.empty(engine.backward_workspace_bytes(zl, n), dtype=torch.uint8, device=dev)
+
+    def fwd_bwd():
+        engine.forward(zl, u, obs_dev, 1, _lib.ZL_PREC_F32, want_comps=False, out_total=total, stream=sh)
+        engine.backward(zl, u, obs_dev, 1, g_total=g_up, grad_out=grad, workspace=ws, stream=sh)
+
+    def bwd_only():
+        engine.backward(zl, u, obs_dev, 1, g_total=g_up, grad_out=grad, workspace=ws, stream=sh)
+
+    def timed_fn(fn, k, w):
+        for _ in range(w):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            ts.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ts) / k
+
+    fb_ms = timed_fn(fwd_bwd, max(2, min(args.steps, 5)), 2)
+    bwd_ms = timed_fn(bwd_only, max(2, min(args.steps, 5)), 1)
+
     # ---- XU roofline --------------------------------------------------------
     sink = torch.empty(8 * 1024, dtype=torch.float32, device=dev)
     ops = _lib.ctypes.c_double(0)
@@ -376,7 +406,10 @@ def main():
             "fp64_ms_per_step": ms64,
             "speedup_fp32_vs_fp64": ms64 / ms32,
             "rel_err_fp32_vs_fp64": err,
-            "fwd_bwd_ms": None,
+            "fwd_bwd_ms": fb_ms,
+            "bwd_ms": bwd_ms,
+            "fwd_bwd_over_fwd": fb_ms / ms32,
+            "n_params": int(grad.numel()),
             "roofline": {
                 "bound": "xu",
                 "achieved": xu_achieved / 1e9,

@@ -138,6 +138,40 @@ ZL_API int zl_forward(const ZlModel* model, const double* unit_vectors_dev, int6
                const ZlObserver* observers_dev, int32_t n_obs, int32_t precision,
                double* out_comps_dev, double* out_total_dev, void* stream);
 
+/* ---- Adjoint -------------------------------------------------------------
+ * Gradient of a loss L with respect to every model parameter, given the
+ * upstream gradient dL/d(output) of the float32 forward pass (no counterpart
+ * in the reference, which has no derivatives; parameters and their order follow
+ * the reference's parameter dictionary, zodipy/zodiacal_light_model.py:38-55).
+ * Gradient vector layout (float64):
+ *   per component c, in model order: d/d x_0, y_0, z_0, i [deg], Omega [deg],
+ *     n_0, then cloud: alpha, beta, gamma, mu | band: delta_zeta [deg], v, p,
+ *     delta_r | ring: R, sigma_r, sigma_z | feature: R, sigma_r, sigma_z,
+ *     theta [deg], sigma_theta [deg]
+ *   d/d T_0, d/d delta
+ *   per spectral set s: d/d emissivity[c] (c = 0..n_comps-1), d/d albedo[c],
+ *     d/d C1, C2, C3, d/d solar_irradiance (the interpolated scalars)
+ * Supported for the built-in component layouts (DIRBE: cloud, 3 bands, ring,
+ * feature; Planck: cloud, 3 bands).  The sum over pixels is deterministic:
+ * fixed 128-pixel tiles reduced in a fixed order, independent of the launch. */
+
+/* Number of entries of the gradient vector for this model. */
+ZL_API int zl_grad_count(const ZlModel* model, int32_t* count);
+
+/* Device workspace zl_backward needs for n_pix pixels (the caller allocates it). */
+ZL_API int zl_backward_workspace_bytes(const ZlModel* model, int64_t n_pix, size_t* bytes);
+
+/* Backward pass.  Exactly one of
+ *   g_comps_dev: float64 [n_spec][n_comps][n_pix]  dL/d out_comps
+ *   g_total_dev: float64 [n_spec][n_pix]            dL/d out_total
+ * is non-NULL.  grad_out_dev receives zl_grad_count() float64 values
+ * (overwritten, not accumulated).  workspace_dev holds at least
+ * zl_backward_workspace_bytes() bytes; ZL_ERR_SPACE if it is smaller. */
+ZL_API int zl_backward(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+                       const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
+                       const double* g_total_dev, double* grad_out_dev, void* workspace_dev,
+                       size_t workspace_bytes, void* stream);
+
 /* Launch configuration used by zl_forward for a precision, as chosen by the
  * autotuner (threads per block, blocks per SM; 0 = library default). */
 ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);

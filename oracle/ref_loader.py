@@ -155,7 +155,7 @@ class _V:
 
 def reference_evaluate(
     ref: types.SimpleNamespace,
-    model_name: str,
+    model_name,
     unit_vectors: np.ndarray,
     obs_xyz: np.ndarray,
     earth_xyz: np.ndarray,
@@ -164,6 +164,7 @@ def reference_evaluate(
     weights: np.ndarray | None,
     gauss_quad_degree: int,
     bounds_error: bool = False,
+    scalars: dict | None = None,
 ) -> np.ndarray:
     """Run the reference's own hot path exactly as ``Model._evaluate`` does.
 
@@ -178,7 +179,7 @@ def reference_evaluate(
     """
     import functools
 
-    model = ref.model_registry.model_registry.get_model(model_name)
+    model = ref.model_registry.model_registry.get_model(model_name) if isinstance(model_name, str) else model_name
     spectrum = _V(np.asarray(model.spectrum))
     x = _V(x_in_model_units)
     w = None if weights is None else _V(weights)
@@ -205,6 +206,14 @@ def reference_evaluate(
         if model.solar_irradiance is not None
         else 0
     )
+
+    if scalars is not None:  # explicit interpolated spectral scalars (for derivatives)
+        for idx, label in enumerate(model.comps):
+            comp_params[label] = {"emissivity": scalars["emissivity"][idx], "albedo": scalars["albedo"][idx]}
+        for key in ("C1", "C2", "C3", "solar_irradiance"):
+            shared[key] = scalars[key]
+        shared["T_0"] = scalars.get("T_0", shared["T_0"])
+        shared["delta"] = scalars.get("delta", shared["delta"])
 
     obs = np.asarray(obs_xyz, dtype=np.float64)
     if obs.ndim == 1:
@@ -259,3 +268,59 @@ def reference_spectral_scalars(ref, model_name, x_in_model_units, weights, bound
         else 0.0
     )
     return out
+
+
+def reference_fd_gradient(ref, model_name, u, obs, earth, bb_table, x_model, weights, degree, a, rel_step=1e-5):
+    """Central finite differences of L = sum_i a_i total_i through the reference's own code.
+
+    Parameters are the component init parameters (``to_dict`` order, angles in
+    degrees), T_0, delta, and the interpolated spectral scalars (emissivity and
+    albedo per component, C1, C2, C3, solar irradiance).  The step is
+    ``rel_step * max(|p|, 1)``.  Returns (names, gradient, loss).
+    """
+    import dataclasses
+
+    base = ref.model_registry.model_registry.get_model(model_name)
+    scal = reference_spectral_scalars(ref, model_name, x_model, weights)
+    scal = {k: (list(v) if isinstance(v, list) else v) for k, v in scal.items()}
+    scal["T_0"], scal["delta"] = float(base.T_0), float(base.delta)
+
+    def loss(model, sc):
+        out = reference_evaluate(ref, model, u, obs, earth, bb_table, x_model, weights, degree, scalars=sc)
+        return float(np.dot(a, out.sum(axis=0)))
+
+    names, grads = [], []
+    L0 = loss(base, scal)
+    for label, comp in base.comps.items():
+        init = {f.name: getattr(comp, f.name) for f in dataclasses.fields(comp) if f.init}
+        for key, val in init.items():
+            h = rel_step * max(abs(float(val)), 1.0)
+            vals = []
+            for sgn in (1, -1):
+                comps = dict(base.comps)
+                comps[label] = type(comp)(**{**init, key: float(val) + sgn * h})
+                vals.append(loss(dataclasses.replace(base, comps=comps), scal))
+            names.append(f"comps.{label.value}.{key}")
+            grads.append((vals[0] - vals[1]) / (2 * h))
+    for key in ("T_0", "delta"):
+        h = rel_step * max(abs(scal[key]), 1.0)
+        vals = [loss(base, {**scal, key: scal[key] + sgn * h}) for sgn in (1, -1)]
+        names.append(key)
+        grads.append((vals[0] - vals[1]) / (2 * h))
+    for key in ("emissivity", "albedo"):
+        for idx, label in enumerate(base.comps):
+            v0 = scal[key][idx]
+            h = rel_step * max(abs(v0), 1.0)
+            vals = []
+            for sgn in (1, -1):
+                lst = list(scal[key])
+                lst[idx] = v0 + sgn * h
+                vals.append(loss(base, {**scal, key: lst}))
+            names.append(f"{key}.{label.value}")
+            grads.append((vals[0] - vals[1]) / (2 * h))
+    for key in ("C1", "C2", "C3", "solar_irradiance"):
+        h = rel_step * max(abs(scal[key]), 1.0)
+        vals = [loss(base, {**scal, key: scal[key] + sgn * h}) for sgn in (1, -1)]
+        names.append(key)
+        grads.append((vals[0] - vals[1]) / (2 * h))
+    return names, np.asarray(grads), L0

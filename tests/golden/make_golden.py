@@ -32,7 +32,13 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 from oracle import zodi_oracle  # noqa: E402
-from oracle.ref_loader import DEFAULT_REF_ROOT, load_reference, reference_evaluate, reference_spectral_scalars  # noqa: E402
+from oracle.ref_loader import (  # noqa: E402
+    DEFAULT_REF_ROOT,
+    load_reference,
+    reference_evaluate,
+    reference_fd_gradient,
+    reference_spectral_scalars,
+)
 from zodipy_gb300.ephemeris import earth_position, iso_to_mjd  # noqa: E402
 from zodipy_gb300.healpix import pix2vec_ring, random_sphere  # noqa: E402
 
@@ -222,6 +228,31 @@ def main() -> None:
         ref_total=ref_tot,
         tabulated=tab,
     )
+    # finite-difference gradients of L = sum_i a_i total_i through the reference itself
+    grad_cases = {
+        "dirbe25": ("dirbe", 25.0, "micron", random_sphere(24, seed=21), [0.9833, 0.0, 0.0], earth_2022),
+        "dirbe1p25": ("dirbe", 1.25, "micron", random_sphere(24, seed=22), earth_1990, earth_1990),
+        "planck18_857": ("planck18", 857.0, "GHz", random_sphere(24, seed=23), [np.cos(2.0), np.sin(2.0), 0.013], earth_2022),
+    }
+    for key, (name, x, unit, u, obs, earth) in grad_cases.items():
+        obs = np.asarray(obs, dtype=np.float64)
+        bb = zodi_oracle.planck_table(x, None, unit=unit)
+        xm = to_model_units(x, unit, name)
+        a = np.random.default_rng(99).uniform(0.5, 1.5, u.shape[1])
+        names, grad, L0 = reference_fd_gradient(ref, name, u, obs, earth, bb, xm, None, 50, a)
+        np.savez_compressed(
+            os.path.join(HERE, f"grad_{key}.npz"),
+            model=np.array(name),
+            x=np.atleast_1d(np.float64(x)),
+            user_unit=np.array(unit),
+            unit_vectors=u,
+            obs=obs,
+            earth=np.asarray(earth, dtype=np.float64),
+            weights_a=a,
+            names=np.array(names),
+            fd_grad=grad,
+            loss=np.array(L0),
+        )
     print("wrote fixtures to", HERE)
 
 

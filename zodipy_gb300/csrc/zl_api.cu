@@ -17,6 +17,15 @@ cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, cons
 cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
                            const ZlObserver* obs, int n_obs, double* oc, double* ot, cudaStream_t st, int tpb,
                            int bps, int num_sms);
+int grad_count_layout(int layout, int n_spec);
+int grad_single_count(int layout);
+int grad_shared_count(int layout);
+cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
+                           const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                           int spec_index, double* partials, int64_t n_tiles, cudaStream_t st, int bps,
+                           int num_sms);
+cudaError_t launch_reduce_tiles(const double* partials, int64_t n_tiles, int ng, double* out, cudaStream_t st);
+cudaError_t launch_gather_spec(const double* red, int n_spec, int ng1, int n_shared, double* out, cudaStream_t st);
 }  // namespace zl
 
 using namespace zl;
@@ -318,5 +327,152 @@ extern "C" ZL_API int zl_forward(const ZlModel* model, const double* u, int64_t 
                        st, cfg.tpb, bps, nsm);
   }
   if (e != cudaSuccess) return cuda_fail(e, "zl_forward launch");
+  return ZL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kBwdTile = 128;
+
+int64_t bwd_tiles(int64_t n_pix) { return (n_pix + kBwdTile - 1) / kBwdTile; }
+
+int bwd_layout(const ZlModel& m, int* layout) {
+  const int l = detect_layout(m);
+  if (l == 0)
+    return fail(ZL_ERR_MODEL,
+                "the adjoint supports the built-in component layouts (cloud, 3 bands[, ring, feature]); "
+                "this model has %d components in another arrangement", m.n_comps);
+  *layout = l;
+  return ZL_OK;
+}
+
+void build_aux(const ZlModel& m, int s, KGradAux* A) {
+  memset(A, 0, sizeof(*A));
+  const double deg = M_PI / 180.0;
+  for (int c = 0; c < m.n_comps; ++c) {
+    const ZlComponent& C = m.comp[c];
+    A->dni[c][0] = (float)(C.sin_Omega * C.cos_i * deg);
+    A->dni[c][1] = (float)(-C.cos_Omega * C.cos_i * deg);
+    A->dni[c][2] = (float)(-C.sin_i * deg);
+    A->dnO[c][0] = (float)(C.cos_Omega * C.sin_i * deg);
+    A->dnO[c][1] = (float)(C.sin_Omega * C.sin_i * deg);
+    A->n0[c] = (float)C.n_0;
+    const double* p = C.p;
+    switch (C.type) {
+      case ZL_CLOUD:
+        for (int k = 0; k < 4; ++k) A->q[c][k] = (float)p[k];
+        break;
+      case ZL_BAND:
+        A->q[c][0] = (float)(p[0] / deg);  // delta_zeta in degrees
+        A->q[c][1] = (float)p[1];
+        A->q[c][2] = (float)p[2];
+        A->q[c][3] = (float)p[3];
+        break;
+      default:
+        A->q[c][0] = (float)p[0];
+        A->q[c][1] = (float)(1.0 / (p[1] * p[1]));
+        A->q[c][2] = (float)(1.0 / p[2]);
+        A->q[c][3] = (float)p[1];
+        A->q[c][4] = (float)p[2];
+        if (C.type == ZL_FEATURE) {
+          A->q[c][5] = (float)(1.0 / (p[4] * p[4]));
+          A->q[c][6] = (float)p[4];
+        }
+    }
+    A->eps[c] = (float)m.spec[s].emissivity[c];
+    A->one_m_alb[c] = (float)(1.0 - m.spec[s].albedo[c]);
+  }
+  const double C1 = m.spec[s].C1, C2 = m.spec[s].C2, C3 = m.spec[s].C3;
+  const double e = std::exp(M_PI * C3), d = C3 * C3 + 1;
+  const double I = 2 * C1 + M_PI * C2 + (e + 1) / d;
+  const double N = 1 / (2 * M_PI * I);
+  const double k = -2 * M_PI * N * N;
+  A->dN[0] = (float)(k * 2);
+  A->dN[1] = (float)(k * M_PI);
+  A->dN[2] = (float)(k * (M_PI * e * d - 2 * C3 * (e + 1)) / (d * d));
+}
+
+}  // namespace
+
+extern "C" ZL_API int zl_grad_count(const ZlModel* model, int32_t* count) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (!count) return fail(ZL_ERR_ARG, "count is NULL");
+  int layout = 0;
+  if ((rc = bwd_layout(*model, &layout))) return rc;
+  *count = grad_count_layout(layout, model->n_spec);
+  return ZL_OK;
+}
+
+extern "C" ZL_API int zl_backward_workspace_bytes(const ZlModel* model, int64_t n_pix, size_t* bytes) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (!bytes || n_pix < 0) return fail(ZL_ERR_ARG, "bytes is NULL or n_pix < 0");
+  int layout = 0;
+  if ((rc = bwd_layout(*model, &layout))) return rc;
+  const int ng1 = grad_single_count(layout);
+  size_t b = (size_t)model->n_spec * (size_t)bwd_tiles(n_pix) * ng1 * sizeof(double);
+  if (model->n_spec > 1) b += (size_t)model->n_spec * ng1 * sizeof(double);
+  *bytes = b;
+  return ZL_OK;
+}
+
+extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs,
+                                  int32_t n_obs, const double* g_comps, const double* g_total, double* grad_out,
+                                  void* workspace, size_t workspace_bytes, void* stream) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  int layout = 0;
+  if ((rc = bwd_layout(*model, &layout))) return rc;
+  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
+  if (!grad_out) return fail(ZL_ERR_ARG, "grad_out is NULL");
+  if (n_pix > 0 && !u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  if ((g_comps == nullptr) == (g_total == nullptr)) return fail(ZL_ERR_ARG, "pass exactly one of g_comps, g_total");
+  size_t need = 0;
+  if ((rc = zl_backward_workspace_bytes(model, n_pix, &need))) return rc;
+  if (workspace_bytes < need || (need > 0 && !workspace))
+    return fail(ZL_ERR_SPACE, "workspace of %zu bytes is smaller than the %zu required", workspace_bytes, need);
+  int nsm = 0;
+  if ((rc = sm_count(&nsm))) return rc;
+  int bps = 0;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    bps = g_cfg[ZL_PREC_F32].bps;
+  }
+  if (bps <= 0) bps = 4;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int ng1 = grad_single_count(layout);
+  const int64_t n_tiles = bwd_tiles(n_pix);
+  double* partials = (double*)workspace;
+  double* red = partials + (size_t)model->n_spec * n_tiles * ng1;
+  static thread_local KParamsF32 P, Ps;
+  static thread_local KGradAux A;
+  build_f32(*model, &P);
+  for (int s = 0; s < model->n_spec; ++s) {
+    Ps = P;
+    Ps.n_spec = 1;
+    Ps.spec[0] = P.spec[s];
+    memcpy(Ps.table[0], P.table[s], sizeof(P.table[0]));
+    Ps.has_scat = 0;
+    for (int c = 0; c < model->n_comps; ++c)
+      if (model->spec[s].albedo[c] != 0.0) Ps.has_scat = 1;
+    build_aux(*model, s, &A);
+    double* part_s = partials + (size_t)s * n_tiles * ng1;
+    cudaError_t e = cudaSuccess;
+    if (n_tiles > 0)
+      e = launch_bwd_f32(Ps, A, layout, u, n_pix, obs, n_obs, g_comps, g_total, s, part_s, n_tiles, st, bps, nsm);
+    if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
+    double* dst = model->n_spec == 1 ? grad_out : red + (size_t)s * ng1;
+    e = launch_reduce_tiles(part_s, n_tiles, ng1, dst, st);
+    if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
+  }
+  if (model->n_spec > 1) {
+    cudaError_t e = launch_gather_spec(red, model->n_spec, ng1, grad_shared_count(layout), grad_out, st);
+    if (e != cudaSuccess) return cuda_fail(e, "zl_backward gather");
+  }
   return ZL_OK;
 }

@@ -1,0 +1,81 @@
+// Float32-path helpers shared by the forward and adjoint kernels.
+#pragma once
+
+#include "zl_common.cuh"
+
+namespace zl {
+
+// Compile-time component layouts.  Nibble c: bit0 present, bit1 first component
+// of a new LOS range, bits 2-3 component type.  LAYOUT 0 = generic (runtime).
+constexpr uint32_t kLayoutDirbe = 0xFB5553u;   // cloud | band band band (same range) | ring | feature
+constexpr uint32_t kLayoutPlanck = 0x5553u;    // cloud | band band band
+constexpr uint32_t kLayoutGeneric = 0u;
+
+template <uint32_t LAYOUT>
+struct Lay {
+  static constexpr bool generic = (LAYOUT == 0u);
+  __host__ __device__ static constexpr int ncomp() {
+    if (generic) return ZL_MAX_COMPS;
+    int n = 0;
+    for (int c = 0; c < ZL_MAX_COMPS; ++c)
+      if ((LAYOUT >> (4 * c)) & 1u) n = c + 1;
+    return n;
+  }
+  __host__ __device__ static constexpr int type(int c) { return (int)((LAYOUT >> (4 * c + 2)) & 3u); }
+  __host__ __device__ static constexpr bool first(int c) { return ((LAYOUT >> (4 * c + 1)) & 1u) != 0; }
+  // LOS-range index of component c: ranges are numbered in order of first use
+  __host__ __device__ static constexpr int range(int c) {
+    int r = -1;
+    for (int j = 0; j <= c; ++j)
+      if (first(j)) ++r;
+    return r;
+  }
+};
+
+// Root of |obs + s u| = cutoff (line_of_sight.py:80-85) in float-float; b omits
+// z_obs u_z like the reference.  At b == 0 the root is taken with sign(+0).
+__device__ __forceinline__ ff sphere_distance_ff(ff b, ff r2, ff cut2) {
+  const ff c = ff_add(r2, ff_neg(cut2));
+  const ff D = ff_add(ff_mul(b, b), ff_scale(c, -4.0f));
+  const ff sq = ff_sqrt(D);
+  const ff q = ff_scale(ff_add(b, (b.hi < 0.f || (b.hi == 0.f && signbit(b.hi))) ? ff_neg(sq) : sq), -0.5f);
+  const ff cq = ff_div(c, q);
+  if (isnan(q.hi) || isnan(cq.hi)) return {q.hi + cq.hi, 0.f};
+  return (q.hi > cq.hi || (q.hi == cq.hi && q.lo >= cq.lo)) ? q : cq;
+}
+
+__device__ __forceinline__ float bb_lookup(const float4* __restrict__ tab, float T, float t_min, float t_max,
+                                           float inv_dt, int nT) {
+  const float Tc = fminf(fmaxf(T, t_min), t_max);
+  int j = floor_nonneg((Tc - t_min) * inv_dt);
+  j = min(j, nT - 2);
+  const float4 e = tab[j];  // (T_j, B_j, slope_j, -)
+  return fmaf(e.z, Tc - e.x, e.y);
+}
+
+// Table value and its derivative dB/dT: the slope of the segment holding T, and
+// 0 where numpy.interp clamps (T outside the table).
+__device__ __forceinline__ float2 bb_lookup_d(const float4* __restrict__ tab, float T, float t_min, float t_max,
+                                              float inv_dt, int nT) {
+  const float Tc = fminf(fmaxf(T, t_min), t_max);
+  int j = floor_nonneg((Tc - t_min) * inv_dt);
+  j = min(j, nT - 2);
+  const float4 e = tab[j];
+  const float slope = (T > t_min && T < t_max) ? e.z : 0.f;
+  return make_float2(fmaf(e.z, Tc - e.x, e.y), slope);
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float t) {
+  const float y = t - c;
+  const float s1 = s + y;
+  c = (s1 - s) - y;
+  s = s1;
+}
+
+// float32 value of hs * x + mid from float-float parts, within ~1 ulp
+__device__ __forceinline__ float node_position(ff hs, ff x, ff mid) {
+  const float r = fmaf(hs.hi, x.hi, mid.hi);
+  return r + fmaf(hs.hi, x.lo, fmaf(hs.lo, x.hi, mid.lo));
+}
+
+}  // namespace zl

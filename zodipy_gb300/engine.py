@@ -83,3 +83,62 @@ def forward(
     )
     _lib.check(rc, "zl_forward")
     return (out_comps if want_comps else None), (out_total if want_total else None)
+
+
+def grad_count(zl_model: _lib.ZlModel) -> int:
+    n = ctypes.c_int32(0)
+    _lib.check(_lib.load().zl_grad_count(ctypes.byref(zl_model), ctypes.byref(n)), "zl_grad_count")
+    return int(n.value)
+
+
+def backward_workspace_bytes(zl_model: _lib.ZlModel, n_pix: int) -> int:
+    b = ctypes.c_size_t(0)
+    _lib.check(
+        _lib.load().zl_backward_workspace_bytes(ctypes.byref(zl_model), int(n_pix), ctypes.byref(b)),
+        "zl_backward_workspace_bytes",
+    )
+    return int(b.value)
+
+
+def backward(
+    zl_model: _lib.ZlModel,
+    u_dev,
+    observers_dev,
+    n_obs: int,
+    g_comps=None,
+    g_total=None,
+    grad_out=None,
+    workspace=None,
+    stream: int | None = None,
+):
+    """Run ``zl_backward``: gradient (float64 CUDA tensor) of the loss w.r.t. the parameter vector."""
+    torch = _torch()
+    if (g_comps is None) == (g_total is None):
+        raise ValueError("pass exactly one of g_comps (n_spec, C, N) or g_total (n_spec, N)")
+    u_dev = u_dev.contiguous()
+    n = u_dev.shape[1]
+    dev = u_dev.device
+    g = (g_comps if g_comps is not None else g_total).to(device=dev, dtype=torch.float64).contiguous()
+    want = (zl_model.n_spec, zl_model.n_comps, n) if g_comps is not None else (zl_model.n_spec, n)
+    if tuple(g.shape) != want:
+        raise ValueError(f"upstream gradient must have shape {want}, got {tuple(g.shape)}")
+    if grad_out is None:
+        grad_out = torch.empty(grad_count(zl_model), dtype=torch.float64, device=dev)
+    need = backward_workspace_bytes(zl_model, n)
+    if workspace is None or workspace.numel() * workspace.element_size() < need:
+        workspace = torch.empty(max(need, 8), dtype=torch.uint8, device=dev)
+    rc = _lib.load().zl_backward(
+        ctypes.byref(zl_model),
+        ctypes.c_void_p(u_dev.data_ptr()),
+        n,
+        ctypes.c_void_p(observers_dev.data_ptr()),
+        n_obs,
+        ctypes.c_void_p(g.data_ptr() if g_comps is not None else 0),
+        ctypes.c_void_p(g.data_ptr() if g_total is not None else 0),
+        ctypes.c_void_p(grad_out.data_ptr()),
+        ctypes.c_void_p(workspace.data_ptr()),
+        workspace.numel() * workspace.element_size(),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(dev)),
+    )
+    _lib.check(rc, "zl_backward")
+    return grad_out

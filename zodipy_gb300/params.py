@@ -1,0 +1,98 @@
+"""The model parameter vector of the adjoint, and its mapping to ``ZlModel``.
+
+The vector follows the gradient layout of ``include/zodigb.h`` (``zl_backward``):
+per component, the reference's parameter-dictionary entries in order
+(``zodipy/zodiacal_light_model.py:38-55``: x_0, y_0, z_0, i, Omega, n_0 and the
+type's own, angles in degrees), then T_0 and delta, then per spectral set the
+interpolated emissivity and albedo of every component, C1, C2, C3 and the solar
+irradiance.  ``vector_from_model`` reads a packed ``ZlModel`` into that vector,
+``model_from_vector`` writes a vector back (re-deriving sin/cos and radians as
+``zodipy/component.py:39-44,87-89,133-136`` does).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+
+_OWN = {
+    _lib.ZL_CLOUD: ("alpha", "beta", "gamma", "mu"),
+    _lib.ZL_BAND: ("delta_zeta", "v", "p", "delta_r"),
+    _lib.ZL_RING: ("R", "sigma_r", "sigma_z"),
+    _lib.ZL_FEATURE: ("R", "sigma_r", "sigma_z", "theta", "sigma_theta"),
+}
+# own parameters that the ZlModel stores in radians but the dictionary holds in degrees
+_DEG = {(_lib.ZL_BAND, 0), (_lib.ZL_FEATURE, 3), (_lib.ZL_FEATURE, 4)}
+
+
+def names(zl_model, labels) -> list[str]:
+    out = []
+    for c in range(zl_model.n_comps):
+        t = zl_model.comp[c].type
+        lab = labels[c]
+        out += [f"comps.{lab}.{k}" for k in ("x_0", "y_0", "z_0", "i", "Omega", "n_0", *_OWN[t])]
+    out += ["T_0", "delta"]
+    for s in range(zl_model.n_spec):
+        sfx = f"[{s}]" if zl_model.n_spec > 1 else ""
+        out += [f"emissivity.{lab}{sfx}" for lab in labels[: zl_model.n_comps]]
+        out += [f"albedo.{lab}{sfx}" for lab in labels[: zl_model.n_comps]]
+        out += [f"C1{sfx}", f"C2{sfx}", f"C3{sfx}", f"solar_irradiance{sfx}"]
+    return out
+
+
+def vector_from_model(m) -> np.ndarray:
+    v = []
+    for c in range(m.n_comps):
+        k = m.comp[c]
+        inc = math.degrees(math.atan2(k.sin_i, k.cos_i))
+        node = math.degrees(math.atan2(k.sin_Omega, k.cos_Omega))
+        v += [k.offset[0], k.offset[1], k.offset[2], inc, node, k.n_0]
+        for j in range(len(_OWN[k.type])):
+            v.append(math.degrees(k.p[j]) if (k.type, j) in _DEG else k.p[j])
+    v += [m.T_0, m.delta]
+    for s in range(m.n_spec):
+        sp = m.spec[s]
+        v += [sp.emissivity[c] for c in range(m.n_comps)]
+        v += [sp.albedo[c] for c in range(m.n_comps)]
+        v += [sp.C1, sp.C2, sp.C3, sp.solar_irradiance]
+    return np.asarray(v, dtype=np.float64)
+
+
+def model_from_vector(base, vec) -> "_lib.ZlModel":
+    """A copy of ``base`` with every vector parameter replaced."""
+    m = _lib.ZlModel.from_buffer_copy(base)
+    vec = np.asarray(vec, dtype=np.float64)
+    j = 0
+    for c in range(m.n_comps):
+        k = m.comp[c]
+        k.offset[0], k.offset[1], k.offset[2] = vec[j : j + 3]
+        inc, node = math.radians(vec[j + 3]), math.radians(vec[j + 4])
+        k.sin_i, k.cos_i = math.sin(inc), math.cos(inc)
+        k.sin_Omega, k.cos_Omega = math.sin(node), math.cos(node)
+        k.n_0 = vec[j + 5]
+        j += 6
+        for q in range(len(_OWN[k.type])):
+            k.p[q] = math.radians(vec[j]) if (k.type, q) in _DEG else vec[j]
+            j += 1
+    m.T_0, m.delta = vec[j], vec[j + 1]
+    j += 2
+    for s in range(m.n_spec):
+        sp = m.spec[s]
+        for c in range(m.n_comps):
+            sp.emissivity[c] = vec[j + c]
+            sp.albedo[c] = vec[j + m.n_comps + c]
+        j += 2 * m.n_comps
+        sp.C1, sp.C2, sp.C3, sp.solar_irradiance = vec[j : j + 4]
+        j += 4
+    if j != vec.size:
+        raise ValueError(f"parameter vector has {vec.size} entries, the model needs {j}")
+    _lib.check(_lib.load().zl_model_check(ctypes.byref(m)), "zl_model_check")
+    return m
+
+
+def size(m) -> int:
+    return sum(6 + len(_OWN[m.comp[c].type]) for c in range(m.n_comps)) + 2 + m.n_spec * (2 * m.n_comps + 4)
