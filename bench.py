@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nside", type=int, default=NSIDE)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
     return p.parse_args()
 
 
@@ -337,6 +338,44 @@ def main():
     fb_ms = timed_fn(fwd_bwd, max(2, min(args.steps, 5)), 2)
     bwd_ms = timed_fn(bwd_only, max(2, min(args.steps, 5)), 1)
 
+    # ---- batched observers: 256 observers, uneven counts, one graph launch -----
+    batched = None
+    if not args.no_batched:
+        import zodipy_gb300 as zg
+        from zodipy_gb300 import units as zu
+        from zodipy_gb300.batch import BatchEvaluator, random_directions_device, uneven_observers
+
+        pm = zg.Model(857 * zu.GHz, name="planck18", gauss_quad_degree=50)
+        bobs, bcounts = uneven_observers(256, seed=2024)
+        nb = int(bcounts.sum())
+        bu = random_directions_device(nb, seed=2025, device=dev)
+        ev = BatchEvaluator(pm.zl_model, bu, bobs, bcounts, workload(args.nside)[2], precision="float32")
+        tpb, bps_b, _ = ev.autotune(sample=1 << 21, reps=2, use_cache=False)
+        ev.capture()
+        for _ in range(2):
+            ev.replay()
+        torch.cuda.synchronize()
+        bt = []
+        for _ in range(max(3, min(args.steps, 5))):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ev.replay()
+            b.record(stream)
+            torch.cuda.synchronize()
+            bt.append(a.elapsed_time(b))
+        bms = sum(bt) / len(bt)
+        batched = {
+            "workload": "planck18 857 GHz, 256 observers on a 1 AU circle (z ~ N(0, 0.01) AU), "
+            f"pixel counts U{{10000..500000}} (seed 2024): {nb} LOS, GL 50, float32, one CUDA-graph launch",
+            "los": nb,
+            "ms_per_launch": bms,
+            "los_per_s": nb / (bms * 1e-3),
+            "autotuned_launch": {"threads_per_block": tpb, "blocks_per_sm": bps_b},
+        }
+        del ev, bu
+        _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, 0), "reset launch")
+
     # ---- XU roofline --------------------------------------------------------
     sink = torch.empty(8 * 1024, dtype=torch.float32, device=dev)
     ops = _lib.ctypes.c_double(0)
@@ -410,6 +449,7 @@ def main():
             "bwd_ms": bwd_ms,
             "fwd_bwd_over_fwd": fb_ms / ms32,
             "n_params": int(grad.numel()),
+            "batched": batched,
             "roofline": {
                 "bound": "xu",
                 "achieved": xu_achieved / 1e9,

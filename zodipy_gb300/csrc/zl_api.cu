@@ -20,6 +20,7 @@ cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry,
 int grad_count_layout(int layout, int n_spec);
 int grad_single_count(int layout);
 int grad_shared_count(int layout);
+int bwd_groups(int layout);
 cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
                            const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
                            int spec_index, double* partials, int64_t n_tiles, cudaStream_t st, int bps,
@@ -53,12 +54,20 @@ struct LaunchCfg {
 LaunchCfg g_cfg[2];
 std::mutex g_mu;
 
+// SM count of the current device, queried once per device and cached so that
+// launches recorded into a CUDA graph make no device queries.
 int sm_count(int* out) {
+  static int cache[64] = {0};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev >= 0 && dev < 64 && cache[dev] > 0) {
+    *out = cache[dev];
+    return ZL_OK;
+  }
   e = cudaDeviceGetAttribute(out, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  if (dev >= 0 && dev < 64) cache[dev] = *out;
   return ZL_OK;
 }
 
@@ -414,7 +423,7 @@ extern "C" ZL_API int zl_backward_workspace_bytes(const ZlModel* model, int64_t 
   int layout = 0;
   if ((rc = bwd_layout(*model, &layout))) return rc;
   const int ng1 = grad_single_count(layout);
-  size_t b = (size_t)model->n_spec * (size_t)bwd_tiles(n_pix) * ng1 * sizeof(double);
+  size_t b = (size_t)model->n_spec * bwd_groups(layout) * (size_t)bwd_tiles(n_pix) * ng1 * sizeof(double);
   if (model->n_spec > 1) b += (size_t)model->n_spec * ng1 * sizeof(double);
   *bytes = b;
   return ZL_OK;
@@ -447,8 +456,9 @@ extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t
   cudaStream_t st = (cudaStream_t)stream;
   const int ng1 = grad_single_count(layout);
   const int64_t n_tiles = bwd_tiles(n_pix);
+  const int64_t rows = n_tiles * bwd_groups(layout);  // partial rows per spectral set
   double* partials = (double*)workspace;
-  double* red = partials + (size_t)model->n_spec * n_tiles * ng1;
+  double* red = partials + (size_t)model->n_spec * rows * ng1;
   static thread_local KParamsF32 P, Ps;
   static thread_local KGradAux A;
   build_f32(*model, &P);
@@ -461,13 +471,13 @@ extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t
     for (int c = 0; c < model->n_comps; ++c)
       if (model->spec[s].albedo[c] != 0.0) Ps.has_scat = 1;
     build_aux(*model, s, &A);
-    double* part_s = partials + (size_t)s * n_tiles * ng1;
+    double* part_s = partials + (size_t)s * rows * ng1;
     cudaError_t e = cudaSuccess;
     if (n_tiles > 0)
       e = launch_bwd_f32(Ps, A, layout, u, n_pix, obs, n_obs, g_comps, g_total, s, part_s, n_tiles, st, bps, nsm);
     if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
     double* dst = model->n_spec == 1 ? grad_out : red + (size_t)s * ng1;
-    e = launch_reduce_tiles(part_s, n_tiles, ng1, dst, st);
+    e = launch_reduce_tiles(part_s, rows, ng1, dst, st);
     if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
   }
   if (model->n_spec > 1) {

@@ -51,7 +51,11 @@ struct GradLay {
   static constexpr int NG = NCP + 2 + 2 * NC + 4;
 };
 
-template <uint32_t LAYOUT>
+// MASK selects the components this launch differentiates (bit c = component c).
+// A model's components are split into groups that each own their LOS ranges, so
+// every group launch carries only its own accumulators; parameters shared by
+// all components (T_0, delta, C1..C3, S) are summed over the groups' partials.
+template <uint32_t LAYOUT, uint32_t MASK>
 __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                         const __grid_constant__ KGradAux A,
                                                         const double* __restrict__ u, int64_t n_pix,
@@ -91,7 +95,10 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
 #pragma unroll
       for (int r = 0; r < ZL_MAX_RANGES; ++r) {
-        if (r < nr) {
+        bool used = false;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
+        if (used && r < nr) {
           const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
                                                     : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
           const ff sp = ((outside >> (2 * r + 1)) & 1u)
@@ -113,6 +120,8 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       ff a2_c[NC], a1_c[NC], a0_c[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
+        un_c[c] = on_c[c] = gup[c] = 0.f;
+        if (!((MASK >> c) & 1u)) continue;
         const KCompF32& C = P.comp[c];
         const int type = L::type(c);
         const ff hs = hs_r[L::range(c)], md = mid_r[L::range(c)];
@@ -162,6 +171,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
         float Bv = 0.f, dB = 0.f, Tn = 0.f, T = 0.f, sf = 0.f, flux = 0.f, base = 0.f, theta = 0.f, eC3 = 0.f;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
+          if (!((MASK >> c) & 1u)) continue;
           const KCompF32& C = P.comp[c];
           const int type = L::type(c);
           if (L::first(c)) {
@@ -374,6 +384,10 @@ int grad_shared_count(int layout) {
   return -1;
 }
 
+// Component groups per layout: DIRBE = {cloud, bands} + {ring, feature}; Planck = one group.
+int bwd_groups(int layout) { return layout == 1 ? 2 : 1; }
+
+// partials: [bwd_groups(layout)][n_tiles][NG] for this spectral set
 cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
                            const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
                            int spec_index, double* partials, int64_t n_tiles, cudaStream_t st, int bps,
@@ -381,12 +395,18 @@ cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, c
   int64_t grid = (int64_t)num_sms * bps;
   if (grid > n_tiles) grid = n_tiles;
   if (grid < 1) grid = 1;
-  if (layout == 1)
-    bwd_f32_kernel<kLayoutDirbe><<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total,
-                                                                    spec_index, partials, n_tiles);
-  else
-    bwd_f32_kernel<kLayoutPlanck><<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total,
-                                                                     spec_index, partials, n_tiles);
+  if (layout == 1) {
+    constexpr int NG = GradLay<kLayoutDirbe>::NG;
+    bwd_f32_kernel<kLayoutDirbe, 0x0Fu><<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total,
+                                                                          spec_index, partials, n_tiles);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    bwd_f32_kernel<kLayoutDirbe, 0x30u><<<(unsigned)grid, kTile, 0, st>>>(
+        P, A, u, n, obs, n_obs, g_comps, g_total, spec_index, partials + (size_t)n_tiles * NG, n_tiles);
+  } else {
+    bwd_f32_kernel<kLayoutPlanck, 0x0Fu><<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total,
+                                                                           spec_index, partials, n_tiles);
+  }
   return cudaGetLastError();
 }
 
