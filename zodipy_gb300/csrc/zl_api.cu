@@ -370,25 +370,29 @@ void build_aux(const ZlModel& m, int s, KGradAux* A) {
     A->dnO[c][1] = (float)(C.sin_Omega * C.sin_i * deg);
     A->n0[c] = (float)C.n_0;
     const double* p = C.p;
+    // derivative constants, with every division done here in float64
     switch (C.type) {
-      case ZL_CLOUD:
+      case ZL_CLOUD:  // alpha, beta, gamma, mu, 1/mu
         for (int k = 0; k < 4; ++k) A->q[c][k] = (float)p[k];
+        A->q[c][4] = (float)(1.0 / p[3]);
         break;
-      case ZL_BAND:
-        A->q[c][0] = (float)(p[0] / deg);  // delta_zeta in degrees
+      case ZL_BAND:  // delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
+        A->q[c][0] = (float)(p[0] / deg);
         A->q[c][1] = (float)p[1];
         A->q[c][2] = (float)p[2];
         A->q[c][3] = (float)p[3];
+        A->q[c][4] = (float)(deg / p[0]);
+        A->q[c][5] = (float)(-20.0 / p[3]);
         break;
-      default:
+      default:  // R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
         A->q[c][0] = (float)p[0];
         A->q[c][1] = (float)(1.0 / (p[1] * p[1]));
         A->q[c][2] = (float)(1.0 / p[2]);
-        A->q[c][3] = (float)p[1];
-        A->q[c][4] = (float)p[2];
+        A->q[c][3] = (float)(2.0 / (p[1] * p[1] * p[1]));
+        A->q[c][4] = (float)(1.0 / (p[2] * p[2]));
         if (C.type == ZL_FEATURE) {
           A->q[c][5] = (float)(1.0 / (p[4] * p[4]));
-          A->q[c][6] = (float)p[4];
+          A->q[c][6] = (float)(2.0 * deg / (p[4] * p[4] * p[4]));
         }
     }
     A->eps[c] = (float)m.spec[s].emissivity[c];

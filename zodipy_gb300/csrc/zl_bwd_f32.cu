@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           // dens = n0 * du; GR = d ln n / d R_c, GZ = d ln n / d Z; p6.. = d ln n / d (own params)
           float du, GR, GZ, p6 = 0.f, p7 = 0.f, p8 = 0.f, p9 = 0.f, p10 = 0.f, dthx = 0.f, dthy = 0.f;
           if (type == ZL_CLOUD) {
-            // q: alpha, beta, gamma, mu
+            // q: alpha, beta, gamma, mu, 1/mu
             const float zeta = aZ * rcinv;
             const bool in = zeta < q[3];
             const float g = in ? zeta * zeta * C.c[5] : zeta - C.c[6];
@@ -222,15 +222,16 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             const float gg = ex2_ftz(q[2] * lgg);
             du = ex2_ftz(-q[0] * lg2Rc - C.c[2] * gg);
             const float bgg = q[1] * q[2] * gg;
-            const float Az = zeta > 0.f ? bgg * (in ? 2.f / zeta : 1.f / g) : 0.f;
+            const float rg = __fdividef(1.f, g);  // g > 0 wherever it is used below
+            const float Az = zeta > 0.f ? bgg * (in ? __fdividef(2.f, zeta) : rg) : 0.f;
             GR = (-q[0] + Az * zeta) * rcinv;
             GZ = -Az * sZ * rcinv;
             p6 = -lg2Rc * kLn2;
             p7 = -gg;
             p8 = g > 0.f ? -q[1] * gg * lgg * kLn2 : 0.f;
-            p9 = in ? bgg / q[3] : (g > 0.f ? 0.5f * bgg / g : 0.f);
+            p9 = in ? bgg * q[4] : (g > 0.f ? 0.5f * bgg * rg : 0.f);
           } else if (type == ZL_BAND) {
-            // q: delta_zeta [deg], v, p, delta_r
+            // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
             const float x = aZ * rcinv * C.c[1];
             const float x2 = x * x, x6 = x2 * x2 * x2;
             const float t2 = ex2_ftz(-kLog2e * x6);
@@ -245,17 +246,17 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             const float t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
                                        : 1.f - emy;
             du = 3.f * rcinv * t2 * t3 * t4;
-            const float it3 = 1.f / t3;
-            const float Sx = -6.f * x6 + q[2] * xpv * it3;        // x d ln n / d x
-            const float Y4 = t4 > 0.f ? y * emy / t4 : 1.f;       // y d ln(1 - e^-y) / d y
+            const float it3 = __fdividef(1.f, t3);
+            const float Sx = -6.f * x6 + q[2] * xpv * it3;                  // x d ln n / d x
+            const float Y4 = t4 > 0.f ? y * emy * __fdividef(1.f, t4) : 1.f;  // y d ln(1 - e^-y) / d y
             GR = (-1.f - Sx + 20.f * Y4) * rcinv;
-            GZ = aZ > 0.f ? Sx * sZ / aZ : 0.f;
-            p6 = -Sx / q[0];
-            p7 = -xpv * it3 / q[1];
+            GZ = aZ > 0.f ? Sx * sZ * __fdividef(1.f, aZ) : 0.f;
+            p6 = -Sx * q[4];
+            p7 = -xpv * it3 * C.c[2];
             p8 = x > 0.f ? xpv * lgx * kLn2 * it3 : 0.f;
-            p9 = -20.f * Y4 / q[3];
+            p9 = Y4 * q[5];
           } else {
-            // q: R, 1/sigma_r^2, 1/sigma_z, sigma_r, sigma_z, 1/sigma_theta^2 [rad], sigma_theta [rad]
+            // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
             float dR = Rc - q[0];
             const ff D2 = ff_add_fast(ff_mul(ff_add_fast(ff_mul(a2_c[c], xk), a1_c[c]), xk), a0_c[c]);
             dR = dR + (D2.hi - dR * (Rc + q[0])) * (0.5f * rcinv);
@@ -263,17 +264,17 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             GR = -2.f * dR * q[1];
             GZ = -sZ * q[2];
             p6 = 2.f * dR * q[1];                 // d/d R
-            p7 = 2.f * dR * dR * q[1] / q[3];     // d/d sigma_r
-            p8 = aZ * q[2] / q[4];                // d/d sigma_z
+            p7 = dR * dR * q[3];                  // d/d sigma_r = 2 dR^2 / sigma_r^3
+            p8 = aZ * q[4];                       // d/d sigma_z = |Z| / sigma_z^2
             if (type == ZL_FEATURE) {
               const float dth = atan2f(fmaf(Rl, ruy[c], roy[c]), fmaf(Rl, rux[c], rox[c]));
               arg = fmaf(dth * dth, q[5], arg);
               const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
               p9 = -gth * kDeg;                      // dtheta/dtheta_deg = -pi/180
-              p10 = 2.f * dth * dth * q[5] / q[6] * kDeg;
-              const float rho2 = Xc0 * Xc0 + Xc1 * Xc1;
-              dthx = gth * (Xc1 / rho2 - eqx[c]);
-              dthy = gth * (-Xc0 / rho2 - eqy[c]);
+              p10 = dth * dth * q[6];                // 2 dth^2 / sigma_theta^3 per degree
+              const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
+              dthx = gth * (Xc1 * rr - eqx[c]);
+              dthy = gth * (-Xc0 * rr - eqy[c]);
             }
             du = ex2_ftz(-kLog2e * arg);
           }
