@@ -172,6 +172,19 @@ ZL_API int zl_backward(const ZlModel* model, const double* unit_vectors_dev, int
                        const double* g_total_dev, double* grad_out_dev, void* workspace_dev,
                        size_t workspace_bytes, void* stream);
 
+/* Backward pass without a caller-allocated workspace, for callers that cannot
+ * allocate device memory (a host that owns all device memory through its own
+ * pool, an allocation-free real-time loop, a binding without an allocator).
+ * No counterpart in the reference.  Same inputs and outputs as zl_backward;
+ * the scratch is a 32 MiB array inside the library, held by every GPU that
+ * loads it until exit.  Returns ZL_ERR_SPACE when zl_backward_workspace_bytes()
+ * exceeds 32 MiB (single-band DIRBE: up to 3.4 million pixels).  Calls that
+ * overlap on the GPU share the array and race: serialise them.  The first call
+ * on a device looks up the array's address; make it before any stream capture. */
+ZL_API int zl_backward_static(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+                              const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
+                              const double* g_total_dev, double* grad_out_dev, void* stream);
+
 /* Launch configuration used by zl_forward for a precision, as chosen by the
  * autotuner (threads per block, blocks per SM; 0 = library default). */
 ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);

@@ -102,6 +102,20 @@ _SIGNATURES = {
         ],
     ),
     "zl_set_launch": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "zl_backward_static": (
+        ctypes.c_int,
+        [
+            ctypes.POINTER(ZlModel),
+            ctypes.c_void_p,
+            ctypes.c_int64,
+            ctypes.c_void_p,
+            ctypes.c_int32,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+        ],
+    ),
     "zl_grad_count": (ctypes.c_int, [ctypes.POINTER(ZlModel), ctypes.POINTER(ctypes.c_int32)]),
     "zl_backward_workspace_bytes": (ctypes.c_int, [ctypes.POINTER(ZlModel), ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "zl_backward": (

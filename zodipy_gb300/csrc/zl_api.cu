@@ -32,8 +32,21 @@ cudaError_t launch_gather_spec(const double* red, int n_spec, int ng1, int n_sha
 using namespace zl;
 
 namespace {
-
 thread_local char g_err[512] = "";
+}  // namespace
+
+namespace zl {
+// Record the calling thread's last error (read back with zl_last_error) and return code.
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+}  // namespace zl
+
+namespace {
 
 int fail(int code, const char* fmt, ...) {
   va_list ap;
