@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       }
 
       float un_c[NC], on_c[NC], gup[NC], rux[NC], ruy[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];
-      ff a2_c[NC], a1_c[NC], a0_c[NC];
+      ff wm_c[NC], cw_c[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         un_c[c] = on_c[c] = gup[c] = 0.f;
@@ -136,15 +136,13 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
         gup[c] = (float)(g_comps ? g_comps[((int64_t)spec_index * NC + c) * n_pix + i]
                                  : g_total[(int64_t)spec_index * n_pix + i]) *
                  (hs.hi + hs.lo);
-        a2_c[c] = a1_c[c] = a0_c[c] = ff{0.f, 0.f};
+        wm_c[c] = cw_c[c] = ff{0.f, 0.f};
         rux[c] = ruy[c] = rox[c] = roy[c] = eqx[c] = eqy[c] = 0.f;
         if (type == ZL_RING || type == ZL_FEATURE) {
           const ff beta = C.zero_offset ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
           const ff d2 = C.zero_offset ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-          const ff gamma = ff_add(d2, ff_neg(ff{C.c[4], C.c[5]}));
-          a2_c[c] = ff_mul(hs, hs);
-          a1_c[c] = ff_scale(ff_mul(hs, ff_add(md, beta)), 2.0f);
-          a0_c[c] = ff_add(ff_mul(md, ff_add(md, ff_scale(beta, 2.0f))), gamma);
+          wm_c[c] = ff_add(md, beta);
+          cw_c[c] = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
         }
         if (type == ZL_FEATURE) {
           const float ex = (float)(O.earth[0] - (double)C.ox), ey = (float)(O.earth[1] - (double)C.oy);
@@ -258,8 +256,8 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           } else {
             // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
             float dR = Rc - q[0];
-            const ff D2 = ff_add_fast(ff_mul(ff_add_fast(ff_mul(a2_c[c], xk), a1_c[c]), xk), a0_c[c]);
-            dR = dR + (D2.hi - dR * (Rc + q[0])) * (0.5f * rcinv);
+            const float D2 = sq_plus_ff(lin_ff2(hs_r[L::range(c)], xk, wm_c[c]), cw_c[c]);
+            dR = dR + (D2 - dR * (Rc + q[0])) * (0.5f * rcinv);
             float arg = dR * dR * q[1] + aZ * q[2];
             GR = -2.f * dR * q[1];
             GZ = -sZ * q[2];

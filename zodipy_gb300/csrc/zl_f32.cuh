@@ -72,10 +72,28 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float t) {
   s = s1;
 }
 
-// float32 value of hs * x + mid from float-float parts, within ~1 ulp
-__device__ __forceinline__ float node_position(ff hs, ff x, ff mid) {
-  const float r = fmaf(hs.hi, x.hi, mid.hi);
-  return r + fmaf(hs.hi, x.lo, fmaf(hs.lo, x.hi, mid.lo));
+// float32 value of a * x + b from float-float parts, within ~1 ulp of the result
+// even when the two terms cancel: the FMA forms a.hi x.hi + b.hi exactly before
+// its single rounding, and the low-part terms are first-order corrections.
+__device__ __forceinline__ float lin_ff(ff a, ff x, ff b) {
+  const float r = fmaf(a.hi, x.hi, b.hi);
+  return r + fmaf(a.hi, x.lo, fmaf(a.lo, x.hi, b.lo));
+}
+
+__device__ __forceinline__ float node_position(ff hs, ff x, ff mid) { return lin_ff(hs, x, mid); }
+
+// a * x + b as an unevaluated float-float sum (exact TwoProd of the high parts,
+// TwoSum with b.hi, low-part terms added once)
+__device__ __forceinline__ ff lin_ff2(ff a, ff x, ff b) {
+  const float p = a.hi * x.hi;
+  const float pe = fmaf(a.hi, x.hi, -p);
+  const ff s = ff_two_sum(p, b.hi);
+  return ff_quick(s.hi, s.lo + (pe + fmaf(a.hi, x.lo, fmaf(a.lo, x.hi, b.lo))));
+}
+
+// w^2 + c to ~1 ulp of the result: the FMA squares w.hi exactly
+__device__ __forceinline__ float sq_plus_ff(ff w, ff c) {
+  return fmaf(w.hi, w.hi, c.hi) + fmaf(2.f * w.hi, w.lo, c.lo);
 }
 
 }  // namespace zl

@@ -6,11 +6,12 @@
 //    per pixel in float-float (~48-bit) arithmetic;
 //  - for the ring and the feature (zodipy/number_density.py:113-181), whose
 //    radial profiles are narrow (sigma_r = 0.025 AU), R^2 - R0^2 at each node is
-//    a float-float quadratic in the node abscissa with per-pixel coefficients,
-//    and R - R0 is recovered from it with one Newton step, so the Gaussian
-//    exponent keeps float32 relative accuracy;
-//  - heights above each symmetry plane are linear in the node position with
-//    float-float per-pixel coefficients;
+//    w^2 + c' with w = R_los + u.(X_obs - X_0) carried in float-float and c' a
+//    per-pixel float-float constant, and R - R0 is recovered from it with one
+//    Newton step, so the Gaussian exponent keeps float32 relative accuracy;
+//  - heights above each symmetry plane are linear in the node abscissa with
+//    float-float per-pixel coefficients, evaluated to ~1 ulp with one FMA on
+//    the high parts plus first-order low-part corrections;
 //  - everything else runs in float32 with single MUFU instructions (ex2, lg2,
 //    rsqrt), integer powers by squaring and 1 - e^-y by its series where it
 //    would cancel;
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
     }
 
     // per-component set-up
-    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], a2_c[NC], a1_c[NC], a0_c[NC];
+    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], wm_c[NC], cw_c[NC];
     float ocx[NC], ocy[NC], ocz[NC], rux[NC], ruy[NC], rox[NC], roy[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
@@ -107,17 +108,15 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
       z1_c[c] = ff_mul(hs, un);
       z0_c[c] = ff_add(ff_mul(md, un), on);
-      a2_c[c] = a1_c[c] = a0_c[c] = ff{0.f, 0.f};
+      wm_c[c] = cw_c[c] = ff{0.f, 0.f};
       rux[c] = ruy[c] = rox[c] = roy[c] = 0.f;
       if (PRECISE && (type == ZL_RING || type == ZL_FEATURE)) {
-        // R^2 - R0^2 = a2 x^2 + a1 x + a0 with R_los = hs x + mid,
-        // beta = u . (X_obs - X_0), gamma = |X_obs - X_0|^2 - R0^2
+        // |X - X_0|^2 - R0^2 = (R_los + beta)^2 + (|X_obs - X_0|^2 - beta^2 - R0^2)
+        //                   = w^2 + c',  w = hs x + (mid + beta),  beta = u . (X_obs - X_0)
         const ff beta = C.zero_offset ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
         const ff d2 = C.zero_offset ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-        const ff gamma = ff_add(d2, ff_neg(ff{C.c[4], C.c[5]}));
-        a2_c[c] = ff_mul(hs, hs);
-        a1_c[c] = ff_scale(ff_mul(hs, ff_add(md, beta)), 2.0f);
-        a0_c[c] = ff_add(ff_mul(md, ff_add(md, ff_scale(beta, 2.0f))), gamma);
+        wm_c[c] = ff_add(md, beta);
+        cw_c[c] = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
       }
       if (type == ZL_FEATURE) {
         // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
@@ -197,8 +196,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           Rc = Rc2 * rcinv;
           lg2Rc = 0.5f * lg2_ftz(Rc2);
         }
-        const ff Zff = ff_add_fast(ff_mul(z1_c[c], xk), z0_c[c]);
-        const float Z = Zff.hi + Zff.lo;
+        const float Z = lin_ff(z1_c[c], xk, z0_c[c]);
         float dens;
         if (type == ZL_CLOUD) {  // number_density.py:60-73
           const float zeta = fabsf(Z) * rcinv;
@@ -232,9 +230,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
         } else {  // ring (number_density.py:136-139) and feature (:167-181)
           float dR = Rc - C.c[1];
           if (precise) {
-            // R^2 - R0^2 from the float-float quadratic; one Newton step on R
-            const ff D2 = ff_add_fast(ff_mul(ff_add_fast(ff_mul(a2_c[c], xk), a1_c[c]), xk), a0_c[c]);
-            dR = dR + (D2.hi - dR * (Rc + C.c[1])) * (0.5f * rcinv);
+            // R^2 - R0^2 = w^2 + c' to ~1 ulp; one Newton step on R
+            const float D2 = sq_plus_ff(lin_ff2(hs_c[c], xk, wm_c[c]), cw_c[c]);
+            dR = dR + (D2 - dR * (Rc + C.c[1])) * (0.5f * rcinv);
           }
           float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
           if (type == ZL_FEATURE) {
