@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--nside", type=int, default=NSIDE)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--large", action="store_true", help="config 5: nside 2048 x 3 observers x 3 bands, GL 100")
+    p.add_argument("--large-nside", type=int, default=2048)
     return p.parse_args()
 
 
@@ -215,10 +217,120 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def large_run(args):
+    """Config 5: DIRBE at 12/25/60 um fused, HEALPix nside 2048 x 3 observers (0/120/240 deg on
+    the 1 AU circle), GL 100, float32 forward + adjoint of a per-pixel L2 loss against a
+    perturbed-parameter float64 GPU map.  Also the full-size float32-vs-float64 error."""
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import _build, _lib, engine, packing, params
+    from zodipy_gb300 import units as zu
+    from zodipy_gb300.autograd import fuse_models
+    from zodipy_gb300.ephemeris import earth_position, iso_to_mjd
+    from zodipy_gb300.healpix import pix2vec_ring_torch
+
+    _build.build()
+    _lib.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    nside = args.large_nside
+    models = [zg.Model(w * zu.micron, name="dirbe", gauss_quad_degree=100) for w in (12.0, 25.0, 60.0)]
+    zl = fuse_models(models)
+    umap = pix2vec_ring_torch(nside, dev)
+    npix = umap.shape[1]
+    u = umap.repeat(1, 3).contiguous()
+    del umap
+    n = u.shape[1]
+    ang = np.radians([0.0, 120.0, 240.0])
+    obs = np.stack([np.cos(ang), np.sin(ang), np.zeros(3)])
+    earth = earth_position(iso_to_mjd(OBSTIME))
+    tab = packing.observer_table(zl, obs, earth, np.array([0, npix, 2 * npix]), any_mode=False)
+    obs_dev = engine.upload_observers(tab, dev)
+
+    def ev_time(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b)
+
+    theta0 = params.vector_from_model(zl)
+    rng = np.random.default_rng(5)
+    theta_true = theta0 * (1 + 0.02 * rng.standard_normal(theta0.size))
+    zl_true = params.model_from_vector(zl, theta_true)
+    # target: float64 GPU map at perturbed parameters
+    (_, d), t64 = ev_time(lambda: engine.forward(zl_true, u, obs_dev, 3, _lib.ZL_PREC_F64, want_comps=False))
+    # full-size float32 vs float64 at the same parameters
+    (_, m_true), _ = ev_time(lambda: engine.forward(zl_true, u, obs_dev, 3, _lib.ZL_PREC_F32, want_comps=False))
+    rel = ((m_true - d).abs() / d.abs()).flatten()
+    err_max = float(rel.max())
+    err_med = float(rel[:: max(1, rel.numel() // (1 << 24))].median())
+    del rel, m_true
+    total = torch.empty((3, n), dtype=torch.float64, device=dev)
+    grad = torch.empty(engine.grad_count(zl), dtype=torch.float64, device=dev)
+    ws = torch.empty(engine.backward_workspace_bytes(zl, n), dtype=torch.uint8, device=dev)
+    g = torch.empty_like(total)
+
+    def fwd():
+        engine.forward(zl, u, obs_dev, 3, _lib.ZL_PREC_F32, want_comps=False, out_total=total)
+
+    def bwd():
+        torch.sub(total, d, out=g)
+        g.mul_(2.0)  # d/dm sum (m - d)^2
+        engine.backward(zl, u, obs_dev, 3, g_total=g, grad_out=grad, workspace=ws)
+
+    for _ in range(args.warmup):
+        fwd()
+        bwd()
+    torch.cuda.synchronize()
+    tf, tb = [], []
+    for _ in range(args.steps):
+        _, a = ev_time(fwd)
+        _, b = ev_time(bwd)
+        tf.append(a)
+        tb.append(b)
+    fms, bms = sum(tf) / len(tf), sum(tb) / len(tb)
+    loss = float(((total - d) ** 2).sum())
+    line = {
+        "metric": "LOS/s, DIRBE 12/25/60um fused, nside 2048 x 3 observers, GL 100: fwd and fwd+bwd",
+        "value": n / (fms * 1e-3),
+        "unit": "LOS/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": fms + bms,
+        "higher_is_better": True,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": f"DIRBE 12/25/60 um fused (one launch), HEALPix nside {nside} ({npix} LOS) x 3 observers "
+            f"at 0/120/240 deg on the 1 AU circle = {n} LOS, GL 100, float32 forward + adjoint of "
+            "sum (m - d)^2, d = float64 GPU map at parameters p (1 + 0.02 xi)",
+            "l2": f"inputs {u.numel() * 8 / 1e9:.1f} GB > L2",
+        },
+        "fwd_ms": fms,
+        "bwd_ms": bms,
+        "fwd_bwd_over_fwd": (fms + bms) / fms,
+        "n_params": int(grad.numel()),
+        "loss": loss,
+        "fp64_map_ms": t64,
+        "fp64_los_per_s": n / (t64 * 1e-3),
+        "rel_err_fp32_vs_fp64_full": {"max": err_max, "median": err_med, "values": 3 * n},
+        "gpu_launches": args.steps * (1 + 3 * 2 + 3),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.large:
+        large_run(args)
         return
     rank, world, local_rank = dist_env()
 

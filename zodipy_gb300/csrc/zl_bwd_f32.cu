@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             X2 = fmaf(Rl, uzf, ozf);
             R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
             rinv = rsqrt_ftz(R2);
-            rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
+            if (type == ZL_CLOUD || type == ZL_BAND) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
             R = R2 * rinv;
             lg2R = lg2_ftz(R);
             Tn = ex2_ftz(P.neg_delta * lg2R);
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           if (!C.zero_offset) {
             Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
             rcinv = rsqrt_ftz(Rc2);
-            rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
+            if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
             Rc = Rc2 * rcinv;
             lg2Rc = 0.5f * lg2_ftz(Rc2);
           }

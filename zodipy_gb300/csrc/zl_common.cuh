@@ -189,14 +189,6 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
   return r;
 }
 
-// floor of a non-negative float below 2^22 without the conversion pipe
-__device__ __forceinline__ int floor_nonneg(float t) {
-  float m = t + 8388608.0f;  // 2^23: the mantissa now holds round(t)
-  int j = __float_as_int(m) - 0x4B000000;
-  float r = m - 8388608.0f;
-  return j - (r > t ? 1 : 0);
-}
-
 // ---------------------------------------------------------------------------
 // Binary search of the observer that owns pixel `i` (records sorted by pix_begin).
 // ---------------------------------------------------------------------------

@@ -47,7 +47,7 @@ __device__ __forceinline__ ff sphere_distance_ff(ff b, ff r2, ff cut2) {
 __device__ __forceinline__ float bb_lookup(const float4* __restrict__ tab, float T, float t_min, float t_max,
                                            float inv_dt, int nT) {
   const float Tc = fminf(fmaxf(T, t_min), t_max);
-  int j = floor_nonneg((Tc - t_min) * inv_dt);
+  int j = __float2int_rd((Tc - t_min) * inv_dt);
   j = min(j, nT - 2);
   const float4 e = tab[j];  // (T_j, B_j, slope_j, -)
   return fmaf(e.z, Tc - e.x, e.y);
@@ -58,7 +58,7 @@ __device__ __forceinline__ float bb_lookup(const float4* __restrict__ tab, float
 __device__ __forceinline__ float2 bb_lookup_d(const float4* __restrict__ tab, float T, float t_min, float t_max,
                                               float inv_dt, int nT) {
   const float Tc = fminf(fmaxf(T, t_min), t_max);
-  int j = floor_nonneg((Tc - t_min) * inv_dt);
+  int j = __float2int_rd((Tc - t_min) * inv_dt);
   j = min(j, nT - 2);
   const float4 e = tab[j];
   const float slope = (T > t_min && T < t_max) ? e.z : 0.f;

@@ -168,7 +168,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           X2 = fmaf(Rl, uzf, ozf);
           R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
           rinv = rsqrt_ftz(R2);
-          rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);  // one Newton step
+          // one Newton step where 1/R feeds the bands' e^-(zeta/dzeta)^6 (sensitivity 6 x^6);
+          // the ring/feature distance is corrected from R^2 - R0^2 below instead
+          if (type == ZL_CLOUD || type == ZL_BAND) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
           R = R2 * rinv;
           lg2R = lg2_ftz(R);
           const float T = P.T0 * ex2_ftz(P.neg_delta * lg2R);  // blackbody.py:16-30
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           const float Xc2 = fmaf(Rl, uzf, ocz[c]);
           Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
           rcinv = rsqrt_ftz(Rc2);
-          rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
+          if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
           Rc = Rc2 * rcinv;
           lg2Rc = 0.5f * lg2_ftz(Rc2);
         }

@@ -75,3 +75,49 @@ def random_sphere(n: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     v = rng.standard_normal((3, int(n)))
     return v / np.linalg.norm(v, axis=0)
+
+
+def pix2vec_ring_torch(nside: int, device="cuda"):
+    """(3, 12 nside^2) float64 RING pixel centres computed on the device (same formulas as pix2vec_ring)."""
+    import torch
+
+    nside = int(nside)
+    n_pix = npix(nside)
+    p = torch.arange(n_pix, dtype=torch.int64, device=device)
+    ncap = 2 * nside * (nside - 1)
+    fact = 1.0 / (3.0 * nside * nside)
+    z = torch.empty(n_pix, dtype=torch.float64, device=device)
+    omz = torch.empty_like(z)
+    phi = torch.empty_like(z)
+
+    north = p < ncap
+    pn = p[north]
+    i = (1 + torch.floor(torch.sqrt(1.0 + 2.0 * pn.double())).long()) // 2
+    i = torch.where(2 * i * (i - 1) > pn, i - 1, i)
+    i = torch.where(2 * (i + 1) * i <= pn, i + 1, i)
+    j = pn + 1 - 2 * i * (i - 1)
+    o = i.double() ** 2 * fact
+    omz[north], z[north] = o, 1.0 - o
+    phi[north] = (j.double() - 0.5) * torch.pi / (2.0 * i.double())
+
+    south = p >= n_pix - ncap
+    ps = n_pix - p[south]
+    i = (1 + torch.floor(torch.sqrt(2.0 * ps.double() - 1.0)).long()) // 2
+    i = torch.where(2 * i * (i - 1) >= ps, i - 1, i)
+    i = torch.where(2 * (i + 1) * i < ps, i + 1, i)
+    j = 4 * i + 1 - (ps - 2 * i * (i - 1))
+    o = i.double() ** 2 * fact
+    z[south], omz[south] = o - 1.0, 2.0 - o
+    phi[south] = (j.double() - 0.5) * torch.pi / (2.0 * i.double())
+
+    belt = ~(north | south)
+    pb = p[belt] - ncap
+    i = pb // (4 * nside) + nside
+    j = pb % (4 * nside) + 1
+    s = (i - nside + 1) % 2
+    zb = (2.0 * nside - i.double()) * 2.0 / (3.0 * nside)
+    z[belt], omz[belt] = zb, 1.0 - zb
+    phi[belt] = (j.double() - s.double() / 2.0) * torch.pi / (2.0 * nside)
+
+    st = torch.sqrt(omz * (1.0 + z))
+    return torch.stack([st * torch.cos(phi), st * torch.sin(phi), z])
