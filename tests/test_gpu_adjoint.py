@@ -131,7 +131,8 @@ def test_adjoint_deterministic_across_launch_shapes(lib):
 
 def test_adjoint_fused_equals_sum_of_single_bands(lib):
     """A two-band launch gives the sum of the single-band gradients for shared parameters
-    and each band's own block for the spectral ones, bit for bit."""
+    (to float32 accumulation accuracy: the fused pass forms sum_s g_s e_s per node) and
+    each band's own block for the spectral ones."""
     import torch
 
     from zodipy_gb300 import engine, packing
@@ -149,10 +150,12 @@ def test_adjoint_fused_equals_sum_of_single_bands(lib):
         obs1 = engine.upload_observers(tab)
         singles.append(engine.backward(m1, adj.u, obs1, 1, g_total=g[s : s + 1].contiguous()).cpu().numpy())
     n_shared = fused.size - 2 * (2 * zl.n_comps + 4)
-    np.testing.assert_array_equal(fused[:n_shared], singles[0][:n_shared] + singles[1][:n_shared])
+    summed = singles[0][:n_shared] + singles[1][:n_shared]
+    scale = np.abs(singles[0][:n_shared]) + np.abs(singles[1][:n_shared])
+    assert np.all(np.abs(fused[:n_shared] - summed) <= 1e-5 * scale + 1e-7 * scale.max())
     per = 2 * zl.n_comps + 4
-    np.testing.assert_array_equal(fused[n_shared : n_shared + per], singles[0][n_shared:])
-    np.testing.assert_array_equal(fused[n_shared + per :], singles[1][n_shared:])
+    np.testing.assert_allclose(fused[n_shared : n_shared + per], singles[0][n_shared:], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(fused[n_shared + per :], singles[1][n_shared:], rtol=1e-6, atol=1e-12)
 
 
 def test_adjoint_component_and_total_upstream_agree(lib):

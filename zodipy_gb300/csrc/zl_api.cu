@@ -18,15 +18,11 @@ cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry,
                            const ZlObserver* obs, int n_obs, double* oc, double* ot, cudaStream_t st, int tpb,
                            int bps, int num_sms);
 int grad_count_layout(int layout, int n_spec);
-int grad_single_count(int layout);
-int grad_shared_count(int layout);
 int bwd_groups(int layout);
 cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
                            const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
-                           int spec_index, double* partials, int64_t n_tiles, cudaStream_t st, int bps,
-                           int num_sms);
-cudaError_t launch_reduce_tiles(const double* partials, int64_t n_tiles, int ng, double* out, cudaStream_t st);
-cudaError_t launch_gather_spec(const double* red, int n_spec, int ng1, int n_shared, double* out, cudaStream_t st);
+                           double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms);
+cudaError_t launch_reduce_tiles(const double* partials, int64_t n_rows, int ng, double* out, cudaStream_t st);
 }  // namespace zl
 
 using namespace zl;
@@ -371,7 +367,7 @@ int bwd_layout(const ZlModel& m, int* layout) {
   return ZL_OK;
 }
 
-void build_aux(const ZlModel& m, int s, KGradAux* A) {
+void build_aux(const ZlModel& m, KGradAux* A) {
   memset(A, 0, sizeof(*A));
   const double deg = M_PI / 180.0;
   for (int c = 0; c < m.n_comps; ++c) {
@@ -408,17 +404,22 @@ void build_aux(const ZlModel& m, int s, KGradAux* A) {
           A->q[c][6] = (float)(2.0 * deg / (p[4] * p[4] * p[4]));
         }
     }
-    A->eps[c] = (float)m.spec[s].emissivity[c];
-    A->one_m_alb[c] = (float)(1.0 - m.spec[s].albedo[c]);
+    for (int s = 0; s < m.n_spec; ++s) {
+      A->eps[s][c] = (float)m.spec[s].emissivity[c];
+      A->one_m_alb[s][c] = (float)(1.0 - m.spec[s].albedo[c]);
+    }
   }
-  const double C1 = m.spec[s].C1, C2 = m.spec[s].C2, C3 = m.spec[s].C3;
-  const double e = std::exp(M_PI * C3), d = C3 * C3 + 1;
-  const double I = 2 * C1 + M_PI * C2 + (e + 1) / d;
-  const double N = 1 / (2 * M_PI * I);
-  const double k = -2 * M_PI * N * N;
-  A->dN[0] = (float)(k * 2);
-  A->dN[1] = (float)(k * M_PI);
-  A->dN[2] = (float)(k * (M_PI * e * d - 2 * C3 * (e + 1)) / (d * d));
+  for (int s = 0; s < m.n_spec; ++s) {
+    // phase normalisation N = 1 / (2 pi I) (scattering.py:53-59) and dN/dC_j = -2 pi N^2 dI/dC_j
+    const double C1 = m.spec[s].C1, C2 = m.spec[s].C2, C3 = m.spec[s].C3;
+    const double e = std::exp(M_PI * C3), d = C3 * C3 + 1;
+    const double I = 2 * C1 + M_PI * C2 + (e + 1) / d;
+    const double N = 1 / (2 * M_PI * I);
+    const double k = -2 * M_PI * N * N;
+    A->dN[s][0] = (float)(k * 2);
+    A->dN[s][1] = (float)(k * M_PI);
+    A->dN[s][2] = (float)(k * (M_PI * e * d - 2 * C3 * (e + 1)) / (d * d));
+  }
 }
 
 }  // namespace
@@ -439,10 +440,8 @@ extern "C" ZL_API int zl_backward_workspace_bytes(const ZlModel* model, int64_t 
   if (!bytes || n_pix < 0) return fail(ZL_ERR_ARG, "bytes is NULL or n_pix < 0");
   int layout = 0;
   if ((rc = bwd_layout(*model, &layout))) return rc;
-  const int ng1 = grad_single_count(layout);
-  size_t b = (size_t)model->n_spec * bwd_groups(layout) * (size_t)bwd_tiles(n_pix) * ng1 * sizeof(double);
-  if (model->n_spec > 1) b += (size_t)model->n_spec * ng1 * sizeof(double);
-  *bytes = b;
+  const int ng = grad_count_layout(layout, model->n_spec);
+  *bytes = (size_t)bwd_groups(layout) * (size_t)bwd_tiles(n_pix) * ng * sizeof(double);
   return ZL_OK;
 }
 
@@ -471,35 +470,18 @@ extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t
   }
   if (bps <= 0) bps = 4;
   cudaStream_t st = (cudaStream_t)stream;
-  const int ng1 = grad_single_count(layout);
+  const int ng = grad_count_layout(layout, model->n_spec);
   const int64_t n_tiles = bwd_tiles(n_pix);
-  const int64_t rows = n_tiles * bwd_groups(layout);  // partial rows per spectral set
   double* partials = (double*)workspace;
-  double* red = partials + (size_t)model->n_spec * rows * ng1;
-  static thread_local KParamsF32 P, Ps;
+  static thread_local KParamsF32 P;
   static thread_local KGradAux A;
   build_f32(*model, &P);
-  for (int s = 0; s < model->n_spec; ++s) {
-    Ps = P;
-    Ps.n_spec = 1;
-    Ps.spec[0] = P.spec[s];
-    memcpy(Ps.table[0], P.table[s], sizeof(P.table[0]));
-    Ps.has_scat = 0;
-    for (int c = 0; c < model->n_comps; ++c)
-      if (model->spec[s].albedo[c] != 0.0) Ps.has_scat = 1;
-    build_aux(*model, s, &A);
-    double* part_s = partials + (size_t)s * rows * ng1;
-    cudaError_t e = cudaSuccess;
-    if (n_tiles > 0)
-      e = launch_bwd_f32(Ps, A, layout, u, n_pix, obs, n_obs, g_comps, g_total, s, part_s, n_tiles, st, bps, nsm);
-    if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
-    double* dst = model->n_spec == 1 ? grad_out : red + (size_t)s * ng1;
-    e = launch_reduce_tiles(part_s, rows, ng1, dst, st);
-    if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
-  }
-  if (model->n_spec > 1) {
-    cudaError_t e = launch_gather_spec(red, model->n_spec, ng1, grad_shared_count(layout), grad_out, st);
-    if (e != cudaSuccess) return cuda_fail(e, "zl_backward gather");
-  }
+  build_aux(*model, &A);
+  cudaError_t e = cudaSuccess;
+  if (n_tiles > 0)
+    e = launch_bwd_f32(P, A, layout, u, n_pix, obs, n_obs, g_comps, g_total, partials, n_tiles, st, bps, nsm);
+  if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
+  e = launch_reduce_tiles(partials, n_tiles * bwd_groups(layout), ng, grad_out, st);
+  if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
   return ZL_OK;
 }

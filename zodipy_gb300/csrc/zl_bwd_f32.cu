@@ -2,14 +2,17 @@
 // every model parameter, recomputing the integrand instead of storing
 // pixels x nodes x components.
 //
-// For out[c, i] = hs_c(i) * sum_k w_k e_c(X_ik) n_c(X_ik) (zodipy/brightness.py:21-56
-// summed as zodipy/line_of_sight.py:55-61) and an upstream gradient g[c, i] =
-// dL/d out[c, i], each thread evaluates one pixel and accumulates, per node,
-//   dL/dp += g hs w * d(e n)/dp
+// For out[s, c, i] = hs_c(i) * sum_k w_k e_sc(X_ik) n_c(X_ik)
+// (zodipy/brightness.py:21-56 summed as zodipy/line_of_sight.py:55-61) and an
+// upstream gradient g[s, c, i] = dL/d out[s, c, i], each thread evaluates one
+// pixel and accumulates, per node,
+//   dL/dp += sum_s g[s,c] hs w * d(e_sc n_c)/dp
 // with analytic derivatives of the Kelsall-98 densities
 // (zodipy/number_density.py:47-181), of T(R) = T0 R^-delta through the
 // blackbody table's segment slope (numpy.interp's derivative; 0 where it
-// clamps), and of the scattering term (zodipy/scattering.py:34-59).
+// clamps), and of the scattering term (zodipy/scattering.py:34-59).  All
+// spectral sets of a fused model share one pass: geometry and densities are
+// evaluated once per node and weighted by E_c = sum_s g[s,c] e_sc.
 //
 // Parameters follow the reference's parameter dictionary
 // (zodipy/zodiacal_light_model.py:38-55): per component, in order,
@@ -31,7 +34,7 @@ constexpr float kLn2 = 0.6931471805599453f;
 constexpr float kDeg = 0.017453292519943295f;  // d(rad)/d(deg)
 constexpr int kTile = 128;
 
-template <uint32_t LAYOUT>
+template <uint32_t LAYOUT, int NSPEC>
 struct GradLay {
   using L = Lay<LAYOUT>;
   static constexpr int NC = L::ncomp();
@@ -45,35 +48,37 @@ struct GradLay {
   }
   static constexpr int NCP = off(NC);
   static constexpr int T0 = NCP, DELTA = NCP + 1;
-  __host__ __device__ static constexpr int eps(int c) { return NCP + 2 + c; }
-  __host__ __device__ static constexpr int alb(int c) { return NCP + 2 + NC + c; }
-  static constexpr int C1 = NCP + 2 + 2 * NC, C2 = C1 + 1, C3 = C1 + 2, S = C1 + 3;
-  static constexpr int NG = NCP + 2 + 2 * NC + 4;
+  static constexpr int PER_SPEC = 2 * NC + 4;
+  __host__ __device__ static constexpr int spec0(int s) { return NCP + 2 + s * PER_SPEC; }
+  __host__ __device__ static constexpr int eps(int c, int s) { return spec0(s) + c; }
+  __host__ __device__ static constexpr int alb(int c, int s) { return spec0(s) + NC + c; }
+  __host__ __device__ static constexpr int C(int j, int s) { return spec0(s) + 2 * NC + j; }  // C1, C2, C3, S
+  static constexpr int NG = NCP + 2 + NSPEC * PER_SPEC;
 };
 
 // MASK selects the components this launch differentiates (bit c = component c).
 // A model's components are split into groups that each own their LOS ranges, so
 // every group launch carries only its own accumulators; parameters shared by
 // all components (T_0, delta, C1..C3, S) are summed over the groups' partials.
-template <uint32_t LAYOUT, uint32_t MASK>
+// SCAT: some component has a non-zero albedo (scattering terms are evaluated).
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT>
 __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                         const __grid_constant__ KGradAux A,
                                                         const double* __restrict__ u, int64_t n_pix,
                                                         const ZlObserver* __restrict__ observers, int n_obs,
                                                         const double* __restrict__ g_comps,
-                                                        const double* __restrict__ g_total, int spec_index,
+                                                        const double* __restrict__ g_total,
                                                         double* __restrict__ partials, int64_t n_tiles) {
   using L = Lay<LAYOUT>;
-  using G = GradLay<LAYOUT>;
+  using G = GradLay<LAYOUT, NSPEC>;
   constexpr int NC = L::ncomp();
   constexpr int NG = G::NG;
-  __shared__ float4 tab_sm[ZL_MAX_TEMPS];
+  __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
   const int nT = P.n_temps;
-  for (int t = threadIdx.x; t < nT; t += blockDim.x) tab_sm[t] = P.table[0][t];
+  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
   __syncthreads();
   const int nr = P.n_ranges;
-  const KSpecF32& S = P.spec[0];
 
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t i = tile * kTile + threadIdx.x;
@@ -111,16 +116,19 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
         }
       }
       float bperp = 0.f;
-      if (P.has_scat) {
+      if (SCAT) {
         const float cx = uyf * ozf - uzf * oyf, cy = uzf * oxf - uxf * ozf, cz = uxf * oyf - uyf * oxf;
         bperp = sqrtf(cx * cx + cy * cy + cz * cz);
       }
 
-      float un_c[NC], on_c[NC], gup[NC], rux[NC], ruy[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];
+      float un_c[NC], on_c[NC], rux[NC], ruy[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];
+      float gup[NC][NSPEC];
       ff wm_c[NC], cw_c[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        un_c[c] = on_c[c] = gup[c] = 0.f;
+        un_c[c] = on_c[c] = 0.f;
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) gup[c][s] = 0.f;
         if (!((MASK >> c) & 1u)) continue;
         const KCompF32& C = P.comp[c];
         const int type = L::type(c);
@@ -132,10 +140,12 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
         const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
         un_c[c] = un.hi + un.lo;
         on_c[c] = on.hi + on.lo;
-        // upstream gradient of this pixel: per component, or the total's for all components
-        gup[c] = (float)(g_comps ? g_comps[((int64_t)spec_index * NC + c) * n_pix + i]
-                                 : g_total[(int64_t)spec_index * n_pix + i]) *
-                 (hs.hi + hs.lo);
+        // upstream gradient of this pixel, times (stop - start)/2: per component, or the total's
+        const float hsf = hs.hi + hs.lo;
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s)
+          gup[c][s] = (float)(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) *
+                      hsf;
         wm_c[c] = cw_c[c] = ff{0.f, 0.f};
         rux[c] = ruy[c] = rox[c] = roy[c] = eqx[c] = eqy[c] = 0.f;
         if (type == ZL_RING || type == ZL_FEATURE) {
@@ -155,7 +165,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           rox[c] = cp * ocx + sp * ocy;
           roy[c] = cp * ocy - sp * ocx;
           const float e2 = ex * ex + ey * ey;
-          eqx[c] = ey / e2;  // d atan2(E - X_0)/d x_0
+          eqx[c] = ey / e2;   // d atan2(E - X_0)/d x_0
           eqy[c] = -ex / e2;  // d atan2(E - X_0)/d y_0
         }
       }
@@ -166,7 +176,10 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
         const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
         const float wk = P.gl_w[k];
         float Rl = 0.f, X0 = 0.f, X1 = 0.f, X2 = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
-        float Bv = 0.f, dB = 0.f, Tn = 0.f, T = 0.f, sf = 0.f, flux = 0.f, base = 0.f, theta = 0.f, eC3 = 0.f;
+        float Tn = 0.f, T = 0.f, flux = 0.f, theta = 0.f;
+        float Bv[NSPEC], dB[NSPEC], sf[NSPEC], base[NSPEC], eC3[NSPEC];
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) Bv[s] = dB[s] = sf[s] = base[s] = eC3[s] = 0.f;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           if (!((MASK >> c) & 1u)) continue;
@@ -184,15 +197,22 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             lg2R = lg2_ftz(R);
             Tn = ex2_ftz(P.neg_delta * lg2R);
             T = P.T0 * Tn;
-            const float2 bd = bb_lookup_d(tab_sm, T, P.t_min, P.t_max, P.inv_dt, nT);
-            Bv = bd.x;
-            dB = bd.y;
-            if (P.has_scat) {
+#pragma unroll
+            for (int s = 0; s < NSPEC; ++s) {
+              const float2 bd = bb_lookup_d(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
+              Bv[s] = bd.x;
+              dB[s] = bd.y;
+            }
+            if (SCAT) {
               theta = atan2f(bperp, -(Rl + beta_h.hi));
               flux = rinv * rinv;
-              eC3 = ex2_ftz(S.C3l2e * theta);
-              base = S.C1 + S.C2 * theta + eC3;
-              sf = S.S * flux * (S.N * base);
+#pragma unroll
+              for (int s = 0; s < NSPEC; ++s) {
+                const KSpecF32& S = P.spec[s];
+                eC3[s] = ex2_ftz(S.C3l2e * theta);
+                base[s] = S.C1 + S.C2 * theta + eC3[s];
+                sf[s] = S.S * flux * (S.N * base[s]);
+              }
             }
           }
           // component frame: X - X_0, its norm, height above the symmetry plane
@@ -209,7 +229,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           const float aZ = fabsf(Z);
           const float sZ = Z > 0.f ? 1.f : (Z < 0.f ? -1.f : 0.f);
           const float* q = A.q[c];
-          // dens = n0 * du; GR = d ln n / d R_c, GZ = d ln n / d Z; p6.. = d ln n / d (own params)
+          // density = n_0 du; GR = d ln n / d R_c, GZ = d ln n / d Z; p6.. = d ln n / d (own params)
           float du, GR, GZ, p6 = 0.f, p7 = 0.f, p8 = 0.f, p9 = 0.f, p10 = 0.f, dthx = 0.f, dthy = 0.f;
           if (type == ZL_CLOUD) {
             // q: alpha, beta, gamma, mu, 1/mu
@@ -261,25 +281,32 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             float arg = dR * dR * q[1] + aZ * q[2];
             GR = -2.f * dR * q[1];
             GZ = -sZ * q[2];
-            p6 = 2.f * dR * q[1];                 // d/d R
-            p7 = dR * dR * q[3];                  // d/d sigma_r = 2 dR^2 / sigma_r^3
-            p8 = aZ * q[4];                       // d/d sigma_z = |Z| / sigma_z^2
+            p6 = 2.f * dR * q[1];  // d/d R
+            p7 = dR * dR * q[3];   // d/d sigma_r = 2 dR^2 / sigma_r^3
+            p8 = aZ * q[4];        // d/d sigma_z = |Z| / sigma_z^2
             if (type == ZL_FEATURE) {
               const float dth = atan2f(fmaf(Rl, ruy[c], roy[c]), fmaf(Rl, rux[c], rox[c]));
               arg = fmaf(dth * dth, q[5], arg);
               const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
-              p9 = -gth * kDeg;                      // dtheta/dtheta_deg = -pi/180
-              p10 = dth * dth * q[6];                // 2 dth^2 / sigma_theta^3 per degree
+              p9 = -gth * kDeg;                     // dtheta/dtheta_deg = -pi/180
+              p10 = dth * dth * q[6];               // 2 dth^2 / sigma_theta^3 per degree
               const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
               dthx = gth * (Xc1 * rr - eqx[c]);
               dthy = gth * (-Xc0 * rr - eqy[c]);
             }
             du = ex2_ftz(-kLog2e * arg);
           }
-          const float e = fmaf(S.alb[c], sf, S.em1[c] * Bv);
-          const float W = wk * gup[c];
-          const float wd = W * A.n0[c] * du;  // W * density
-          const float coef = wd * e;
+          // emission per spectral set and its upstream-weighted sums
+          float E = 0.f, Q = 0.f;
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) {
+            const KSpecF32& S = P.spec[s];
+            const float ev = SCAT ? fmaf(S.alb[c], sf[s], S.em1[c] * Bv[s]) : S.em1[c] * Bv[s];
+            E = fmaf(gup[c][s], ev, E);
+            Q = fmaf(gup[c][s] * S.em1[c], dB[s], Q);
+          }
+          const float wd = wk * A.n0[c] * du;  // w * density; the upstream gradient is in E and Q
+          const float coef = wd * E;
           const int o = G::off(c);
           const float gRr = GR * rcinv;
           acc[o + 0] += coef * (-gRr * Xc0 - GZ * C.nx + dthx);
@@ -287,25 +314,28 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           acc[o + 2] += coef * (-gRr * Xc2 - GZ * C.nz);
           acc[o + 3] += coef * GZ * (Xc0 * A.dni[c][0] + Xc1 * A.dni[c][1] + Xc2 * A.dni[c][2]);
           acc[o + 4] += coef * GZ * (Xc0 * A.dnO[c][0] + Xc1 * A.dnO[c][1]);
-          acc[o + 5] += W * e * du;
+          acc[o + 5] += wk * E * du;
           acc[o + 6] += coef * p6;
           acc[o + 7] += coef * p7;
           acc[o + 8] += coef * p8;
           if (type != ZL_RING) acc[o + 9] += coef * p9;
           if (type == ZL_FEATURE) acc[o + 10] += coef * p10;
-          // emission side
-          acc[G::eps(c)] += wd * A.one_m_alb[c] * Bv;
-          acc[G::alb(c)] += wd * (sf - A.eps[c] * Bv);
-          const float qd = wd * S.em1[c] * dB;
-          acc[G::T0] += qd * Tn;
-          acc[G::DELTA] -= qd * T * lg2R * kLn2;
-          if (P.has_scat) {
-            const float af = wd * S.alb[c] * flux;
-            acc[G::S] += af * S.N * base;
-            const float as = af * S.S;
-            acc[G::C1] += as * (S.N + base * A.dN[0]);
-            acc[G::C2] += as * (S.N * theta + base * A.dN[1]);
-            acc[G::C3] += as * (S.N * theta * eC3 + base * A.dN[2]);
+          acc[G::T0] += wd * Q * Tn;
+          acc[G::DELTA] -= wd * Q * T * lg2R * kLn2;
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) {
+            const KSpecF32& S = P.spec[s];
+            const float wg = wd * gup[c][s];
+            acc[G::eps(c, s)] += wg * A.one_m_alb[s][c] * Bv[s];
+            acc[G::alb(c, s)] += wg * ((SCAT ? sf[s] : 0.f) - A.eps[s][c] * Bv[s]);
+            if (SCAT) {
+              const float af = wg * S.alb[c] * flux;
+              acc[G::C(3, s)] += af * S.N * base[s];
+              const float as = af * S.S;
+              acc[G::C(0, s)] += as * (S.N + base[s] * A.dN[s][0]);
+              acc[G::C(1, s)] += as * (S.N * theta + base[s] * A.dN[s][1]);
+              acc[G::C(2, s)] += as * (S.N * theta * eC3[s] + base[s] * A.dN[s][2]);
+            }
           }
         }
       }
@@ -331,14 +361,14 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
   }
 }
 
-// Sum tile partials column by column in a fixed order: thread t adds tiles
+// Sum partial rows column by column in a fixed order: thread t adds rows
 // t, t + 256, ...; then a fixed tree.
-__global__ void __launch_bounds__(256) reduce_tiles_kernel(const double* __restrict__ partials, int64_t n_tiles,
+__global__ void __launch_bounds__(256) reduce_tiles_kernel(const double* __restrict__ partials, int64_t n_rows,
                                                             int ng, double* __restrict__ out) {
   __shared__ double sm[256];
   const int j = blockIdx.x;
   double s = 0.0;
-  for (int64_t t = threadIdx.x; t < n_tiles; t += 256) s += partials[t * ng + j];
+  for (int64_t t = threadIdx.x; t < n_rows; t += 256) s += partials[t * ng + j];
   sm[threadIdx.x] = s;
   __syncthreads();
   for (int w = 128; w >= 1; w >>= 1) {
@@ -348,75 +378,72 @@ __global__ void __launch_bounds__(256) reduce_tiles_kernel(const double* __restr
   if (threadIdx.x == 0) out[j] = sm[0];
 }
 
-// Multi-spectral gathering: red[s][ng1] -> final layout (shared parameters summed over s in order).
-__global__ void gather_spec_kernel(const double* __restrict__ red, int n_spec, int ng1, int n_shared,
-                                   double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int per_spec = ng1 - n_shared;
-  const int total = n_shared + n_spec * per_spec;
-  if (j >= total) return;
-  if (j < n_shared) {
-    double s = 0.0;
-    for (int k = 0; k < n_spec; ++k) s += red[k * ng1 + j];
-    out[j] = s;
-  } else {
-    const int k = (j - n_shared) / per_spec, r = (j - n_shared) % per_spec;
-    out[j] = red[k * ng1 + n_shared + r];
-  }
-}
-
+// Gradient vector length for a layout (1 = DIRBE, 2 = Planck) and n_spec; -1 otherwise.
 int grad_count_layout(int layout, int n_spec) {
-  if (layout == 1) return GradLay<kLayoutDirbe>::NCP + 2 + n_spec * (2 * 6 + 4);
-  if (layout == 2) return GradLay<kLayoutPlanck>::NCP + 2 + n_spec * (2 * 4 + 4);
-  return -1;
-}
-
-int grad_single_count(int layout) {
-  if (layout == 1) return GradLay<kLayoutDirbe>::NG;
-  if (layout == 2) return GradLay<kLayoutPlanck>::NG;
-  return -1;
-}
-
-int grad_shared_count(int layout) {
-  if (layout == 1) return GradLay<kLayoutDirbe>::NCP + 2;
-  if (layout == 2) return GradLay<kLayoutPlanck>::NCP + 2;
+  if (layout == 1) return GradLay<kLayoutDirbe, 1>::NCP + 2 + n_spec * GradLay<kLayoutDirbe, 1>::PER_SPEC;
+  if (layout == 2) return GradLay<kLayoutPlanck, 1>::NCP + 2 + n_spec * GradLay<kLayoutPlanck, 1>::PER_SPEC;
   return -1;
 }
 
 // Component groups per layout: DIRBE = {cloud, bands} + {ring, feature}; Planck = one group.
 int bwd_groups(int layout) { return layout == 1 ? 2 : 1; }
 
-// partials: [bwd_groups(layout)][n_tiles][NG] for this spectral set
-cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
-                           const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
-                           int spec_index, double* partials, int64_t n_tiles, cudaStream_t st, int bps,
-                           int num_sms) {
-  int64_t grid = (int64_t)num_sms * bps;
-  if (grid > n_tiles) grid = n_tiles;
-  if (grid < 1) grid = 1;
-  if (layout == 1) {
-    constexpr int NG = GradLay<kLayoutDirbe>::NG;
-    bwd_f32_kernel<kLayoutDirbe, 0x0Fu><<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total,
-                                                                          spec_index, partials, n_tiles);
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC>
+static void launch_one(bool scat, const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
+                       const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                       double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
+  if (scat)
+    bwd_f32_kernel<LAYOUT, MASK, NSPEC, true>
+        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles);
+  else
+    bwd_f32_kernel<LAYOUT, MASK, NSPEC, false>
+        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles);
+}
+
+template <uint32_t LAYOUT, int NSPEC>
+static cudaError_t launch_groups(const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
+                                 const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                                 double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
+  const bool scat = P.has_scat != 0;
+  launch_one<LAYOUT, 0x0Fu, NSPEC>(scat, P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles, st, grid);
+  if constexpr (LAYOUT == kLayoutDirbe) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    bwd_f32_kernel<kLayoutDirbe, 0x30u><<<(unsigned)grid, kTile, 0, st>>>(
-        P, A, u, n, obs, n_obs, g_comps, g_total, spec_index, partials + (size_t)n_tiles * NG, n_tiles);
-  } else {
-    bwd_f32_kernel<kLayoutPlanck, 0x0Fu><<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total,
-                                                                           spec_index, partials, n_tiles);
+    constexpr int NG = GradLay<LAYOUT, NSPEC>::NG;
+    launch_one<LAYOUT, 0x30u, NSPEC>(scat, P, A, u, n, obs, n_obs, g_comps, g_total,
+                                     partials + (size_t)n_tiles * NG, n_tiles, st, grid);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_tiles(const double* partials, int64_t n_tiles, int ng, double* out, cudaStream_t st) {
-  reduce_tiles_kernel<<<ng, 256, 0, st>>>(partials, n_tiles, ng, out);
-  return cudaGetLastError();
+// partials: [bwd_groups(layout)][n_tiles][grad_count_layout(layout, n_spec)]
+cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
+                           const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                           double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms) {
+  int64_t grid = (int64_t)num_sms * bps;
+  if (grid > n_tiles) grid = n_tiles;
+  if (grid < 1) grid = 1;
+#define ZL_BWD_CASE(LAY, NS) \
+  return launch_groups<LAY, NS>(P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles, st, grid)
+  if (layout == 1) {
+    switch (P.n_spec) {
+      case 1: ZL_BWD_CASE(kLayoutDirbe, 1);
+      case 2: ZL_BWD_CASE(kLayoutDirbe, 2);
+      case 3: ZL_BWD_CASE(kLayoutDirbe, 3);
+      default: ZL_BWD_CASE(kLayoutDirbe, 4);
+    }
+  }
+  switch (P.n_spec) {
+    case 1: ZL_BWD_CASE(kLayoutPlanck, 1);
+    case 2: ZL_BWD_CASE(kLayoutPlanck, 2);
+    case 3: ZL_BWD_CASE(kLayoutPlanck, 3);
+    default: ZL_BWD_CASE(kLayoutPlanck, 4);
+  }
+#undef ZL_BWD_CASE
 }
 
-cudaError_t launch_gather_spec(const double* red, int n_spec, int ng1, int n_shared, double* out, cudaStream_t st) {
-  const int total = n_shared + n_spec * (ng1 - n_shared);
-  gather_spec_kernel<<<(total + 127) / 128, 128, 0, st>>>(red, n_spec, ng1, n_shared, out);
+cudaError_t launch_reduce_tiles(const double* partials, int64_t n_rows, int ng, double* out, cudaStream_t st) {
+  reduce_tiles_kernel<<<ng, 256, 0, st>>>(partials, n_rows, ng, out);
   return cudaGetLastError();
 }
 
