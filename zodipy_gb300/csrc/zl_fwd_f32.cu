@@ -12,6 +12,11 @@
 //  - heights above each symmetry plane are linear in the node abscissa with
 //    float-float per-pixel coefficients, evaluated to ~1 ulp with one FMA on
 //    the high parts plus first-order low-part corrections;
+//  - distances are never formed from the position vector: |X - X_0|^2 =
+//    w^2 + b^2 with w = R_los + u.(X_obs - X_0) (linear in the node abscissa,
+//    evaluated as above) and b^2 the squared impact parameter (a per-pixel
+//    constant), two non-negative terms, so lines of sight that graze the Sun
+//    keep float32 relative accuracy where R^-alpha is steepest;
 //  - everything else runs in float32 with single MUFU instructions (ex2, lg2,
 //    rsqrt), integer powers by squaring and 1 - e^-y by its series where it
 //    would cancel;
@@ -67,16 +72,15 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       }
     }
 
-    // scattering geometry: |u x X_obs| and u . X_obs (scattering.py:26-31 rewritten as atan2)
-    float bperp = 0.f;
-    if (P.has_scat) {
-      const float cx = uyf * ozf - uzf * oyf, cy = uzf * oxf - uxf * ozf, cz = uxf * oyf - uyf * oxf;
-      bperp = sqrtf(cx * cx + cy * cy + cz * cz);
-    }
+    // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
+    const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
+    const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
+    // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
+    const float bperp = P.has_scat ? sqrtf(b2h) : 0.f;
 
     // per-component set-up
-    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], wm_c[NC], cw_c[NC];
-    float ocx[NC], ocy[NC], ocz[NC], rux[NC], ruy[NC], rox[NC], roy[NC];
+    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], wm_c[NC], cw_c[NC], mh_c[NC];
+    float b2_c[NC], fx1[NC], fx0[NC], fy1[NC], fy0[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       if (c >= nc) break;
@@ -96,11 +100,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       }
       hs_c[c] = hs;
       mid_c[c] = md;
+      mh_c[c] = ff_add(md, beta_h);  // R_los + u . X_obs = hs x + mh
       const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
                dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
-      ocx[c] = dx.hi + dx.lo;
-      ocy[c] = dy.hi + dy.lo;
-      ocz[c] = dz.hi + dz.lo;
       // height above the symmetry plane, linear in the node abscissa x:
       //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
       const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
@@ -108,26 +110,35 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
       z1_c[c] = ff_mul(hs, un);
       z0_c[c] = ff_add(ff_mul(md, un), on);
-      wm_c[c] = cw_c[c] = ff{0.f, 0.f};
-      rux[c] = ruy[c] = rox[c] = roy[c] = 0.f;
-      if (PRECISE && (type == ZL_RING || type == ZL_FEATURE)) {
-        // |X - X_0|^2 - R0^2 = (R_los + beta)^2 + (|X_obs - X_0|^2 - beta^2 - R0^2)
-        //                   = w^2 + c',  w = hs x + (mid + beta),  beta = u . (X_obs - X_0)
+      // |X - X_0|^2 = w^2 + b^2,  w = hs x + (mid + beta),  beta = u . (X_obs - X_0),
+      // b^2 = |X_obs - X_0|^2 - beta^2;  the ring/feature use w^2 + c' with c' = b^2 - R0^2
+      wm_c[c] = mh_c[c];
+      b2_c[c] = b2h;
+      cw_c[c] = ff{0.f, 0.f};
+      if (!C.zero_offset || (PRECISE && (type == ZL_RING || type == ZL_FEATURE))) {
         const ff beta = C.zero_offset ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
         const ff d2 = C.zero_offset ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+        const ff bb = ff_add(d2, ff_neg(ff_mul(beta, beta)));
         wm_c[c] = ff_add(md, beta);
-        cw_c[c] = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+        b2_c[c] = fmaxf(bb.hi + bb.lo, 0.f);
+        cw_c[c] = ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
       }
+      fx1[c] = fx0[c] = fy1[c] = fy0[c] = 0.f;
       if (type == ZL_FEATURE) {
         // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
-        // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2
+        // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
+        // two coordinates that are linear in the node abscissa
         const float phi = atan2f((float)(O.earth[1] - (double)C.oy), (float)(O.earth[0] - (double)C.ox)) + C.c[6];
         float sp, cp;
         sincosf(phi, &sp, &cp);
-        rux[c] = cp * uxf + sp * uyf;
-        ruy[c] = cp * uyf - sp * uxf;
-        rox[c] = cp * ocx[c] + sp * ocy[c];
-        roy[c] = cp * ocy[c] - sp * ocx[c];
+        const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+        const float rux = cp * uxf + sp * uyf, ruy = cp * uyf - sp * uxf;
+        const float rox = cp * ocx + sp * ocy, roy = cp * ocy - sp * ocx;
+        const float h = hs.hi + hs.lo, m = md.hi + md.lo;
+        fx1[c] = h * rux;
+        fx0[c] = fmaf(m, rux, rox);
+        fy1[c] = h * ruy;
+        fy0[c] = fmaf(m, ruy, roy);
       }
     }
 
@@ -145,7 +156,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
     for (int k = 0; k < P.n_nodes; ++k) {
       const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
       const float wk = P.gl_w[k];
-      float Rl = 0.f, X0 = 0.f, X1 = 0.f, X2 = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
+      float wh = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
       float B[NSPEC], sf[NSPEC], t4s[NC];
 #pragma unroll
       for (int s = 0; s < NSPEC; ++s) {
@@ -161,12 +172,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
         const bool first = L::generic ? (C.first_in_range != 0) : L::first(c);
         const bool precise = PRECISE && (type == ZL_RING || type == ZL_FEATURE);
         if (first) {
-          // brightness.py:27-33 — node position, heliocentric distance, temperature
-          Rl = node_position(hs_c[c], xk, mid_c[c]);
-          X0 = fmaf(Rl, uxf, oxf);
-          X1 = fmaf(Rl, uyf, oyf);
-          X2 = fmaf(Rl, uzf, ozf);
-          R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
+          // brightness.py:27-33 — heliocentric distance of the node, R^2 = w^2 + b^2, and temperature
+          wh = lin_ff(hs_c[c], xk, mh_c[c]);
+          R2 = fmaf(wh, wh, b2h);
           rinv = rsqrt_ftz(R2);
           // one Newton step where 1/R feeds the bands' e^-(zeta/dzeta)^6 (sensitivity 6 x^6);
           // the ring/feature distance is corrected from R^2 - R0^2 below instead
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) B[s] = bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
           if (P.has_scat) {  // scattering.py:11-59
-            const float theta = atan2f(bperp, -(Rl + beta_h.hi));
+            const float theta = atan2f(bperp, -wh);
             const float flux = rinv * rinv;
 #pragma unroll
             for (int s = 0; s < NSPEC; ++s) {
@@ -189,10 +197,8 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
         // own distance when the component is offset from the Sun
         float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R;
         if (!C.zero_offset) {
-          const float Xc0 = fmaf(Rl, uxf, ocx[c]);
-          const float Xc1 = fmaf(Rl, uyf, ocy[c]);
-          const float Xc2 = fmaf(Rl, uzf, ocz[c]);
-          Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
+          const float wc = lin_ff(hs_c[c], xk, wm_c[c]);
+          Rc2 = fmaf(wc, wc, b2_c[c]);
           rcinv = rsqrt_ftz(Rc2);
           if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
           Rc = Rc2 * rcinv;
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           }
           float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
           if (type == ZL_FEATURE) {
-            const float dth = atan2f(fmaf(Rl, ruy[c], roy[c]), fmaf(Rl, rux[c], rox[c]));
+            const float dth = atan2f(fmaf(fy1[c], xk.hi, fy0[c]), fmaf(fx1[c], xk.hi, fx0[c]));
             arg = fmaf(dth * dth, C.c[7], arg);
           }
           dens = C.c[0] * ex2_ftz(-arg);
