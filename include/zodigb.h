@@ -185,6 +185,16 @@ ZL_API int zl_backward_static(const ZlModel* model, const double* unit_vectors_d
                               const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
                               const double* g_total_dev, double* grad_out_dev, void* stream);
 
+/* Number densities of every component on a Cartesian mesh, float64
+ * (replaces the evaluation loop of zodipy/number_density.py:482-536).
+ * x_dev[nx], y_dev[ny], z_dev[nz]: heliocentric ecliptic coordinates [AU];
+ * earth_xyz_host[3]: Earth's position (the feature's longitude origin);
+ * out_dev: float64 [n_comps][ny][nx][nz], the layout of
+ * numpy.meshgrid(x, y, z) with its default 'xy' indexing. */
+ZL_API int zl_density_grid(const ZlModel* model, const double* x_dev, int32_t nx, const double* y_dev, int32_t ny,
+                           const double* z_dev, int32_t nz, const double* earth_xyz_host, double* out_dev,
+                           void* stream);
+
 /* Launch configuration used by zl_forward for a precision, as chosen by the
  * autotuner (threads per block, blocks per SM; 0 = library default). */
 ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);

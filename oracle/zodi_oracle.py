@@ -285,6 +285,29 @@ def evaluate(desc: dict, unit_vectors, obs_xyz, earth_xyz, fix_b0=False) -> np.n
     return out
 
 
+def grid_number_density(desc: dict, x, y, z, earth_xyz) -> np.ndarray:
+    """Component densities on ``numpy.meshgrid(x, y, z)`` (``number_density.py:482-536``).
+
+    Returns (C, ny, nx, nz) float64, the reference's layout; ``earth_xyz`` is
+    Earth's heliocentric position (the feature's longitude origin).
+    """
+    grid = np.asarray(np.meshgrid(np.asarray(x, float), np.asarray(y, float), np.asarray(z, float)))
+    earth = np.asarray(earth_xyz, dtype=np.float64).reshape(3, 1, 1, 1)
+    labels = list(desc["labels"])
+    out = np.zeros((len(labels), *grid.shape[1:]))
+    for idx, label in enumerate(labels):
+        comp = desc["comps"][label]
+        geom = component_geometry(comp)
+        geom["X_0"] = geom["X_0"].reshape(3, 1, 1, 1)
+        kind = comp_type(label)
+        with np.errstate(all="ignore"):
+            if kind == "feature":
+                out[idx] = feature_density(grid, comp, geom, earth)
+            else:
+                out[idx] = _DENSITY[kind](grid, comp, geom)
+    return out
+
+
 def evaluate_chunked(desc, unit_vectors, obs_xyz, earth_xyz, nprocesses=1, fix_b0=False):
     """``evaluate`` split over coordinate chunks like ``model.py:182-200``.
 

@@ -16,6 +16,9 @@ those inputs to the per-component emission.  Outputs:
   los_<case>.npz      inputs + reference per-component emission for one call
   dirbe_idl.npz       inputs + reference emission for the DIRBE IDL known-answer
                       points (tests/dirbe_tabulated.py of the reference)
+  grid_<case>.npz     inputs + reference grid_number_density output
+
+``python tests/golden/make_golden.py grid`` regenerates only the grid fixtures.
 """
 
 from __future__ import annotations
@@ -128,9 +131,47 @@ def dirbe_idl_fixture(ref_root: str):
     return vals
 
 
+def make_grids(ref) -> None:
+    """Reference ``grid_number_density`` (number_density.py:482-536) on small meshes.
+
+    The reference asks astropy for Earth's position (bodies.py:53-62); the
+    fixture fixes it instead, by replacing that lookup with the stored vector.
+    """
+    nd = ref.number_density
+    grid_cases = {
+        "dirbe_wide": ("dirbe", np.linspace(-3, 3, 13), np.linspace(-2.5, 2.5, 11), np.linspace(-1, 1, 7), "2022-01-01T00:00:00"),
+        "dirbe_near_earth": ("dirbe", np.linspace(-0.9, -0.1, 17), np.linspace(-1.3, -0.5, 9), np.linspace(-0.1, 0.1, 5), "2022-06-01T00:00:00"),
+        "planck13_wide": ("planck13", np.linspace(0, 5, 10), np.linspace(0, 5, 10), np.linspace(0, 2, 6), "2022-01-01T00:00:00"),
+        "planck18_ring": ("planck18", np.linspace(0.7, 1.3, 8), np.linspace(-1.3, -0.7, 8), np.linspace(-0.05, 0.05, 3), "1990-06-11T00:00:00"),
+    }
+    saved = nd.get_earthpos_inst
+    try:
+        for key, (name, x, y, z, iso) in grid_cases.items():
+            earth = earth_position(iso_to_mjd(iso)).reshape(3)
+            nd.get_earthpos_inst = lambda obstime, ephemeris, e=earth: e.copy()
+            out = nd.grid_number_density(x, y, z, obstime=None, model=name)
+            np.savez_compressed(
+                os.path.join(HERE, f"grid_{key}.npz"),
+                model=np.array(name),
+                x=x,
+                y=y,
+                z=z,
+                obstime=np.array(iso),
+                earth=earth,
+                ref_out=np.asarray(out, dtype=np.float64),
+            )
+    finally:
+        nd.get_earthpos_inst = saved
+
+
 def main() -> None:
     ref_root = os.environ.get("ZODIPY_REF_ROOT", DEFAULT_REF_ROOT)
     ref = load_reference(ref_root)
+    if sys.argv[1:] == ["grid"]:
+        make_grids(ref)
+        print("wrote grid fixtures to", HERE)
+        return
+    make_grids(ref)
     models = dump_models(ref)
     with open(os.path.join(HERE, "ref_models.json"), "w") as f:
         json.dump(models, f, indent=1)

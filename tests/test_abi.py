@@ -103,6 +103,39 @@ def test_forward_argument_errors_need_no_gpu(lib):
     assert lib.zl_forward(ctypes.byref(m), None, 0, obs, 1, 0, None, None, None) == _lib.ZL_OK
 
 
+def test_density_grid_argument_errors_need_no_gpu(lib):
+    from zodipy_gb300 import _lib
+
+    m = _dirbe_zl()
+    e = (ctypes.c_double * 3)(1.0, 0.0, 0.0)
+    p = ctypes.c_void_p(8)
+    assert lib.zl_density_grid(ctypes.byref(m), p, -1, p, 2, p, 2, e, p, None) == _lib.ZL_ERR_ARG
+    assert lib.zl_density_grid(ctypes.byref(m), None, 2, p, 2, p, 2, e, p, None) == _lib.ZL_ERR_ARG
+    assert "NULL" in _lib.last_error()
+    assert lib.zl_density_grid(ctypes.byref(m), p, 2, p, 2, p, 2, None, p, None) == _lib.ZL_ERR_ARG
+    # an empty mesh is a successful no-op
+    assert lib.zl_density_grid(ctypes.byref(m), None, 0, None, 3, None, 3, e, None, None) == _lib.ZL_OK
+    bad = _dirbe_zl()
+    bad.abi_version = 999
+    assert lib.zl_density_grid(ctypes.byref(bad), p, 2, p, 2, p, 2, e, p, None) == _lib.ZL_ERR_MODEL
+
+
+def test_grid_number_density_rejects_bad_model_type():
+    import zodipy_gb300 as zg
+
+    with pytest.raises(TypeError):
+        zg.grid_number_density([0.0], [0.0], [0.0], obstime="2022-01-01", model=2)
+
+
+def test_pack_densities_is_a_valid_model(lib):
+    from zodipy_gb300 import packing
+    from zodipy_gb300.zodiacal_light_model import model_registry
+
+    for name in ("dirbe", "planck18"):
+        m = packing.pack_densities(model_registry.get_model(name))
+        assert m.n_comps == len(model_registry.get_model(name).comps)
+
+
 def test_observer_flags_follow_reference_rule(lib):
     """line_of_sight.py:72-73: a cutoff collapses to eps when r_obs > cutoff (strict)."""
     from zodipy_gb300 import packing

@@ -1,0 +1,112 @@
+"""zl_density_grid (grid_number_density) against the reference's fixtures and the oracle.
+
+Tolerance: the kernel evaluates the reference's expressions in float64 in the
+same order; only the transcendental functions (pow, exp, atan2, sqrt) differ
+from numpy's by a few ulp.  Two amplifications follow:
+
+- exp(-e) with |e| <= 745 before underflow: relative error below
+  745 * 4 * 2.2e-16 ~ 7e-13, covered by rtol 1e-11 (absolute floor 1e-300 for
+  subnormal results);
+- the band factor 1 - exp(-(R / delta_r)^20) (number_density.py:107) cancels
+  for R << delta_r: one ulp of exp near 1 (<= 2.2e-16) becomes a relative error
+  of 2.2e-16 / term4 in the density.  Band points get that much more, with a
+  factor 2 margin (term4 computed here from the grid).
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, cuda_ok, ref_models
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not cuda_ok(), reason="needs CUDA")]
+
+RTOL, ATOL = 1e-11, 1e-300
+GRID_CASES = ["dirbe_wide", "dirbe_near_earth", "planck13_wide", "planck18_ring"]
+
+
+def _band_condition(name, x, y, z):
+    """Per point and component: 4.4e-16 / (1 - exp(-(R/delta_r)^20)) for bands, 0 otherwise."""
+    m = ref_models()[name]
+    X = np.asarray(np.meshgrid(np.asarray(x, float), np.asarray(y, float), np.asarray(z, float)))
+    kappa = np.zeros((len(m["comps"]), *X.shape[1:]))
+    with np.errstate(all="ignore"):
+        for c, (label, comp) in enumerate(m["comps"].items()):
+            if label.startswith("band"):
+                R = np.sqrt((X[0] - comp["x_0"]) ** 2 + (X[1] - comp["y_0"]) ** 2 + (X[2] - comp["z_0"]) ** 2)
+                kappa[c] = 4.4e-16 / -np.expm1(-((R / comp["delta_r"]) ** 20))
+    return kappa
+
+
+def _close(out, ref, kappa):
+    assert out.shape == ref.shape
+    np.testing.assert_array_equal(np.isnan(out), np.isnan(ref))
+    fin = np.isfinite(ref)
+    np.testing.assert_array_equal(np.isfinite(out), fin)
+    a, b, k = out[fin], ref[fin], kappa[fin]
+    bad = np.abs(a - b) > (RTOL + k) * np.abs(b) + ATOL
+    if bad.any():
+        j = np.flatnonzero(bad)[:5]
+        raise AssertionError(f"{bad.sum()} points off: out {a[j]} ref {b[j]} allowed rel {RTOL + k[j]}")
+
+
+def _grid_on_device(name, x, y, z, earth):
+    import torch
+
+    from zodipy_gb300 import engine, packing
+    from zodipy_gb300.zodiacal_light_model import model_registry
+
+    zl = packing.pack_densities(model_registry.get_model(name))
+    xd, yd, zd = (torch.from_numpy(np.asarray(v, dtype=np.float64)).cuda() for v in (x, y, z))
+    return engine.density_grid(zl, xd, yd, zd, earth).cpu().numpy()
+
+
+@pytest.mark.parametrize("key", GRID_CASES)
+def test_grid_matches_reference_fixture(lib, key):
+    z = np.load(os.path.join(GOLDEN, f"grid_{key}.npz"))
+    out = _grid_on_device(str(z["model"]), z["x"], z["y"], z["z"], z["earth"])
+    _close(out, z["ref_out"], _band_condition(str(z["model"]), z["x"], z["y"], z["z"]))
+
+
+def test_grid_public_api_reference_test_shape(lib):
+    """The reference's own test grid (tests/test_model.py:94-104): 100^3 points, dirbe,
+    obstime 2022-01-01; compared point by point with the oracle at the same Earth position."""
+    import zodipy_gb300 as zg
+    from oracle import zodi_oracle as zo
+    from zodipy_gb300 import units as u
+    from zodipy_gb300.ephemeris import iso_to_mjd
+    from zodipy_gb300.model import earth_xyz
+
+    x = np.linspace(0, 5, 100) * u.AU
+    y = np.linspace(0, 5, 100) * u.AU
+    zc = np.linspace(0, 2, 100) * u.AU
+    grid = zg.grid_number_density(x, y, zc, obstime=zg.Time("2022-01-01"))
+    assert grid.sum(axis=0).shape == (100, 100, 100)
+    m = ref_models()["dirbe"]
+    earth = earth_xyz(np.array([iso_to_mjd("2022-01-01")])).reshape(3)
+    ref = zo.grid_number_density({"labels": list(m["comps"]), "comps": m["comps"]}, x.value, y.value, zc.value, earth)
+    _close(grid, ref, _band_condition("dirbe", x.value, y.value, zc.value))
+
+
+def test_grid_device_output_and_units(lib):
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import units as u
+
+    x = np.linspace(-2, 2, 9)
+    au_km = 149597870.7
+    a = zg.grid_number_density(x * u.AU, x * u.AU, x[:5] * u.AU, obstime="2022-03-01", model="planck18", device_output=True)
+    b = zg.grid_number_density(x * au_km * u.km, x, x[:5], obstime="2022-03-01", model="planck18")
+    assert isinstance(a, torch.Tensor) and a.is_cuda and tuple(a.shape) == (4, 9, 9, 5)
+    _close(a.cpu().numpy(), b, _band_condition("planck18", x, x, x[:5]))
+
+
+def test_grid_accepts_model_instance_and_empty_axis(lib):
+    import zodipy_gb300 as zg
+    from zodipy_gb300.zodiacal_light_model import model_registry
+
+    model = model_registry.get_model("dirbe")
+    g = zg.grid_number_density([1.0, 2.0], [0.5], [], obstime="2022-01-01", model=model)
+    assert g.shape == (6, 1, 2, 0)

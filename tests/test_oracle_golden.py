@@ -61,3 +61,29 @@ def test_oracle_chunked_is_partition_independent():
         [zo.evaluate(desc, part, case["obs"], case["earth"]) for part in np.array_split(u, 5, axis=-1)], axis=-1
     )
     np.testing.assert_array_equal(whole, parts)
+
+
+GRID_CASES = ["dirbe_wide", "dirbe_near_earth", "planck13_wide", "planck18_ring"]
+
+
+def grid_desc(name):
+    from conftest import ref_models
+
+    m = ref_models()[name]
+    return {"labels": list(m["comps"]), "comps": m["comps"]}
+
+
+@pytest.mark.parametrize("key", GRID_CASES)
+def test_oracle_grid_matches_reference(key):
+    """grid_number_density restatement vs the reference's own output, bit for bit (nan where R = 0)."""
+    import os
+
+    from conftest import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, f"grid_{key}.npz"))
+    out = zo.grid_number_density(grid_desc(str(z["model"])), z["x"], z["y"], z["z"], z["earth"])
+    ref = z["ref_out"]
+    assert out.shape == ref.shape == (len(grid_desc(str(z["model"]))["labels"]), z["y"].size, z["x"].size, z["z"].size)
+    np.testing.assert_array_equal(np.isnan(out), np.isnan(ref))
+    finite = np.isfinite(ref)
+    np.testing.assert_array_equal(out[finite], ref[finite])

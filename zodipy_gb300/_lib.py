@@ -102,6 +102,21 @@ _SIGNATURES = {
         ],
     ),
     "zl_set_launch": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "zl_density_grid": (
+        ctypes.c_int,
+        [
+            ctypes.POINTER(ZlModel),
+            ctypes.c_void_p,
+            ctypes.c_int32,
+            ctypes.c_void_p,
+            ctypes.c_int32,
+            ctypes.c_void_p,
+            ctypes.c_int32,
+            ctypes.POINTER(ctypes.c_double),
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+        ],
+    ),
     "zl_backward_static": (
         ctypes.c_int,
         [

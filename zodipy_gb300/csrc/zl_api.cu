@@ -23,6 +23,8 @@ cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, c
                            const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
                            double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms);
 cudaError_t launch_reduce_tiles(const double* partials, int64_t n_rows, int ng, double* out, cudaStream_t st);
+cudaError_t launch_density_grid(const ZlModel& M, const double* x, int nx, const double* y, int ny, const double* z,
+                                int nz, double ex, double ey, double* out, cudaStream_t st, int num_sms);
 }  // namespace zl
 
 using namespace zl;
@@ -483,5 +485,24 @@ extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t
   if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
   e = launch_reduce_tiles(partials, n_tiles * bwd_groups(layout), ng, grad_out, st);
   if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
+  return ZL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Densities on a mesh
+// ---------------------------------------------------------------------------
+extern "C" ZL_API int zl_density_grid(const ZlModel* model, const double* x, int32_t nx, const double* y, int32_t ny,
+                                      const double* z, int32_t nz, const double* earth_xyz, double* out,
+                                      void* stream) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (nx < 0 || ny < 0 || nz < 0) return fail(ZL_ERR_ARG, "negative grid size");
+  if ((int64_t)nx * ny * nz == 0) return ZL_OK;
+  if (!x || !y || !z || !out || !earth_xyz) return fail(ZL_ERR_ARG, "NULL pointer argument");
+  int nsm = 0;
+  if ((rc = sm_count(&nsm))) return rc;
+  cudaError_t e = launch_density_grid(*model, x, nx, y, ny, z, nz, earth_xyz[0], earth_xyz[1], out,
+                                      (cudaStream_t)stream, nsm);
+  if (e != cudaSuccess) return cuda_fail(e, "zl_density_grid launch");
   return ZL_OK;
 }

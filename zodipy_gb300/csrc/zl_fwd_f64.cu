@@ -65,6 +65,46 @@ __device__ __forceinline__ double sphere_distance(double b, double r_obs, double
   return np_maximum(q, c / q);
 }
 
+// Number density of one Kelsall-98 component at heliocentric X (zodipy/number_density.py:47-181),
+// every expression in the reference's order; (ex, ey) is Earth's heliocentric x, y (feature only).
+__device__ __forceinline__ double density_f64(const ZlComponent& C, double X0, double X1, double X2, double ex,
+                                              double ey) {
+  // number_density.py: X - X_0, its norm, and the height above the symmetry plane
+  const double Xc0 = X0 - C.offset[0], Xc1 = X1 - C.offset[1], Xc2 = X2 - C.offset[2];
+  const double Rc = sqrt(Xc0 * Xc0 + Xc1 * Xc1 + Xc2 * Xc2);
+  const double Zc = Xc0 * C.sin_Omega * C.sin_i - Xc1 * C.cos_Omega * C.sin_i + Xc2 * C.cos_i;
+  if (C.type == ZL_CLOUD) {  // number_density.py:60-73
+    const double zeta = fabs(Zc / Rc);
+    const double mu = C.p[3];
+    const double g = zeta < mu ? zeta * zeta / (2.0 * mu) : zeta - (mu / 2.0);
+    return C.n_0 * pow(Rc, -C.p[0]) * exp(-C.p[1] * pow(g, C.p[2]));
+  }
+  if (C.type == ZL_BAND) {  // number_density.py:99-110
+    const double zeta = fabs(Zc / Rc);
+    const double zz = zeta / C.p[0];
+    const double t1 = 3.0 * C.n_0 / Rc;
+    const double t2 = exp(-pow(zz, 6.0));
+    const double t3 = 1.0 + pow(zz, C.p[2]) / C.p[1];
+    const double t4 = 1.0 - exp(-pow(Rc / C.p[3], 20.0));
+    return t1 * t2 * t3 * t4;
+  }
+  if (C.type == ZL_RING) {  // number_density.py:136-139
+    const double d = Rc - C.p[0];
+    const double t1 = -(d * d) / (C.p[1] * C.p[1]);
+    const double t2 = fabs(Zc) / C.p[2];
+    return C.n_0 * exp(t1 - t2);
+  }
+  // feature, number_density.py:167-181
+  const double te = atan2(ey - C.offset[1], ex - C.offset[0]);
+  double dth = (atan2(Xc1, Xc0) - te) - C.p[3];
+  dth = np_remainder(dth + kPi, 2.0 * kPi) - kPi;
+  const double d = Rc - C.p[0];
+  double e = d * d / (C.p[1] * C.p[1]);
+  e += fabs(Zc) / C.p[2];
+  e += dth * dth / (C.p[4] * C.p[4]);
+  return C.n_0 * exp(-e);
+}
+
 template <int NSPEC>
 __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KParamsF64 P,
                                                       const double* __restrict__ u, int64_t n_pix,
@@ -156,39 +196,7 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
           }
           hs_len = sp - st;
         }
-        // number_density.py: X - X_0, its norm, and the height above the symmetry plane
-        const double Xc0 = X0 - C.offset[0], Xc1 = X1 - C.offset[1], Xc2 = X2 - C.offset[2];
-        const double Rc = sqrt(Xc0 * Xc0 + Xc1 * Xc1 + Xc2 * Xc2);
-        const double Zc = Xc0 * C.sin_Omega * C.sin_i - Xc1 * C.cos_Omega * C.sin_i + Xc2 * C.cos_i;
-        double dens;
-        if (C.type == ZL_CLOUD) {  // number_density.py:60-73
-          const double zeta = fabs(Zc / Rc);
-          const double mu = C.p[3];
-          const double g = zeta < mu ? zeta * zeta / (2.0 * mu) : zeta - (mu / 2.0);
-          dens = C.n_0 * pow(Rc, -C.p[0]) * exp(-C.p[1] * pow(g, C.p[2]));
-        } else if (C.type == ZL_BAND) {  // number_density.py:99-110
-          const double zeta = fabs(Zc / Rc);
-          const double zz = zeta / C.p[0];
-          const double t1 = 3.0 * C.n_0 / Rc;
-          const double t2 = exp(-pow(zz, 6.0));
-          const double t3 = 1.0 + pow(zz, C.p[2]) / C.p[1];
-          const double t4 = 1.0 - exp(-pow(Rc / C.p[3], 20.0));
-          dens = t1 * t2 * t3 * t4;
-        } else if (C.type == ZL_RING) {  // number_density.py:136-139
-          const double d = Rc - C.p[0];
-          const double t1 = -(d * d) / (C.p[1] * C.p[1]);
-          const double t2 = fabs(Zc) / C.p[2];
-          dens = C.n_0 * exp(t1 - t2);
-        } else {  // feature, number_density.py:167-181
-          const double te = atan2(O.earth[1] - C.offset[1], O.earth[0] - C.offset[0]);
-          double dth = (atan2(Xc1, Xc0) - te) - C.p[3];
-          dth = np_remainder(dth + kPi, 2.0 * kPi) - kPi;
-          const double d = Rc - C.p[0];
-          double e = d * d / (C.p[1] * C.p[1]);
-          e += fabs(Zc) / C.p[2];
-          e += dth * dth / (C.p[4] * C.p[4]);
-          dens = C.n_0 * exp(-e);
-        }
+        const double dens = density_f64(C, X0, X1, X2, O.earth[0], O.earth[1]);
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
           const double A = P.m.spec[s].albedo[c];
@@ -227,6 +235,34 @@ static cudaError_t launch_f64_t(const KParamsF64& P, const double* u, int64_t n,
   if (grid > blocks_needed) grid = blocks_needed;
   if (grid < 1) grid = 1;
   fwd_f64_kernel<NSPEC><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, n_obs, oc, ot);
+  return cudaGetLastError();
+}
+
+// Densities on a Cartesian mesh (zodipy/number_density.py:482-536): point (iy, ix, iz) of
+// numpy.meshgrid(x, y, z) (default 'xy' indexing) is (x[ix], y[iy], z[iz]); out is
+// [n_comps][ny][nx][nz].
+__global__ void __launch_bounds__(256) density_grid_kernel(const __grid_constant__ ZlModel M,
+                                                           const double* __restrict__ x, int nx,
+                                                           const double* __restrict__ y, int ny,
+                                                           const double* __restrict__ z, int nz, double ex, double ey,
+                                                           double* __restrict__ out) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(t % nz);
+    const int ix = (int)((t / nz) % nx);
+    const int iy = (int)(t / ((int64_t)nz * nx));
+    const double X0 = x[ix], X1 = y[iy], X2 = z[iz];
+    for (int c = 0; c < M.n_comps; ++c) out[(int64_t)c * n + t] = density_f64(M.comp[c], X0, X1, X2, ex, ey);
+  }
+}
+
+cudaError_t launch_density_grid(const ZlModel& M, const double* x, int nx, const double* y, int ny, const double* z,
+                                int nz, double ex, double ey, double* out, cudaStream_t st, int num_sms) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  int64_t grid = (n + 255) / 256;
+  if (grid > (int64_t)num_sms * 16) grid = (int64_t)num_sms * 16;
+  if (grid < 1) grid = 1;
+  density_grid_kernel<<<(unsigned)grid, 256, 0, st>>>(M, x, nx, y, ny, z, nz, ex, ey, out);
   return cudaGetLastError();
 }
 

@@ -142,3 +142,33 @@ def backward(
     )
     _lib.check(rc, "zl_backward")
     return grad_out
+
+
+def density_grid(zl_model: _lib.ZlModel, x_dev, y_dev, z_dev, earth_xyz, out=None, stream: int | None = None):
+    """Run ``zl_density_grid``: float64 (C, ny, nx, nz) densities on the mesh of x, y, z (CUDA tensors)."""
+    torch = _torch()
+    for v in (x_dev, y_dev, z_dev):
+        if v.dtype != torch.float64 or not v.is_cuda or v.dim() != 1:
+            raise ValueError("grid coordinates must be 1-D float64 CUDA tensors")
+    x_dev, y_dev, z_dev = x_dev.contiguous(), y_dev.contiguous(), z_dev.contiguous()
+    nx, ny, nz = x_dev.numel(), y_dev.numel(), z_dev.numel()
+    shape = (zl_model.n_comps, ny, nx, nz)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float64, device=x_dev.device)
+    elif tuple(out.shape) != shape or out.dtype != torch.float64 or not out.is_contiguous():
+        raise ValueError(f"out must be a contiguous float64 tensor of shape {shape}")
+    earth = (ctypes.c_double * 3)(*[float(v) for v in np.asarray(earth_xyz, dtype=np.float64).reshape(3)])
+    rc = _lib.load().zl_density_grid(
+        ctypes.byref(zl_model),
+        ctypes.c_void_p(x_dev.data_ptr()),
+        nx,
+        ctypes.c_void_p(y_dev.data_ptr()),
+        ny,
+        ctypes.c_void_p(z_dev.data_ptr()),
+        nz,
+        earth,
+        ctypes.c_void_p(out.data_ptr()),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(x_dev.device)),
+    )
+    _lib.check(rc, "zl_density_grid")
+    return out

@@ -37,6 +37,22 @@ def _astropy():
         return None, None
 
 
+def earth_xyz(mjd, ephemeris: str = "builtin") -> np.ndarray:
+    """Earth's heliocentric ecliptic position (3, n) [AU] (``zodipy/bodies.py:13-24``).
+
+    Uses astropy's ephemerides when astropy is importable, else the built-in
+    analytic ephemeris.
+    """
+    coords, u = _astropy()
+    if coords is not None:
+        from astropy.time import Time
+
+        t = Time(mjd, format="mjd")
+        pos = coords.get_body("earth", t, ephemeris=ephemeris).transform_to(coords.HeliocentricMeanEcliptic)
+        return np.asarray(pos.cartesian.xyz.to_value(u.AU), dtype=np.float64).reshape(3, -1)
+    return body_position("earth", mjd).reshape(3, -1)
+
+
 class Model:
     """Zodiacal light model evaluated on the GPU."""
 
@@ -201,14 +217,7 @@ class Model:
 
     # -- internals -----------------------------------------------------------
     def _earth_position(self, mjd: np.ndarray) -> np.ndarray:
-        coords, u = _astropy()
-        if coords is not None:
-            from astropy.time import Time
-
-            t = Time(mjd, format="mjd")
-            pos = coords.get_body("earth", t, ephemeris=self._ephemeris).transform_to(coords.HeliocentricMeanEcliptic)
-            return np.asarray(pos.cartesian.xyz.to_value(u.AU), dtype=np.float64).reshape(3, -1)
-        return body_position("earth", mjd).reshape(3, -1)
+        return earth_xyz(mjd, self._ephemeris)
 
     def _body_position(self, body: str, mjd: np.ndarray, earth_xyz: np.ndarray) -> np.ndarray:
         body = body.lower()

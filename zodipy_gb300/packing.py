@@ -96,6 +96,18 @@ def pack_model(ipd_model, spectra: list[dict], bb_tables: list[np.ndarray], gl_x
     return m
 
 
+def pack_densities(ipd_model) -> _lib.ZlModel:
+    """``ZlModel`` carrying only the components' geometry, for ``zl_density_grid``.
+
+    The spectral block is a placeholder (one zero spectrum, a two-point table,
+    one node) that satisfies ``zl_model_check``; densities never read it.
+    """
+    zero = {"emissivity": [0.0] * len(ipd_model.comps), "albedo": [0.0] * len(ipd_model.comps)}
+    zero.update(C1=0.0, C2=0.0, C3=0.0, solar_irradiance=0.0)
+    table = np.array([[1.0, 2.0], [0.0, 0.0]])
+    return pack_model(ipd_model, [zero], [table], [0.0], [2.0])
+
+
 def observer_table(model: _lib.ZlModel, obs_xyz: np.ndarray, earth_xyz: np.ndarray, pix_begin, any_mode: bool):
     """ctypes array of ``ZlObserver`` with the cutoff flags filled in."""
     obs_xyz = np.asarray(obs_xyz, dtype=np.float64).reshape(3, -1)
