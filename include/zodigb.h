@@ -6,7 +6,9 @@
  * range (zodipy/line_of_sight.py:64-105), the Gauss-Legendre quadrature
  * (zodipy/line_of_sight.py:55-61) of the Kelsall integrand
  * (zodipy/brightness.py:21-56) with the four Kelsall-98 densities
- * (zodipy/number_density.py:47-181), the blackbody lookup
+ * (zodipy/number_density.py:47-181) or of the Rowan-Robinson & May integrand
+ * (zodipy/brightness.py:59-83) with its eight densities
+ * (zodipy/number_density.py:184-404), the blackbody lookup
  * (zodipy/blackbody.py:16-30 + np.interp) and scattering
  * (zodipy/scattering.py:11-59).  Everything above that seam (units, frames,
  * ephemerides, spectral unpacking) stays in the host language.
@@ -37,7 +39,7 @@
 extern "C" {
 #endif
 
-#define ZL_ABI_VERSION 1
+#define ZL_ABI_VERSION 2
 
 #define ZL_MAX_COMPS 8   /* components per model (DIRBE has 6) */
 #define ZL_MAX_RANGES 8  /* distinct (inner, outer) cutoff pairs per model */
@@ -45,8 +47,18 @@ extern "C" {
 #define ZL_MAX_NODES 128 /* Gauss-Legendre degree */
 #define ZL_MAX_TEMPS 128 /* blackbody table length (the reference uses 100) */
 
-/* Component type codes (zodipy/number_density.py:408-412). */
-enum { ZL_CLOUD = 0, ZL_BAND = 1, ZL_RING = 2, ZL_FEATURE = 3 };
+/* Component type codes (zodipy/number_density.py:406-419). */
+enum {
+  ZL_CLOUD = 0, ZL_BAND = 1, ZL_RING = 2, ZL_FEATURE = 3,      /* Kelsall et al. (1998) */
+  ZL_FAN = 4, ZL_COMET = 5, ZL_INTERSTELLAR = 6,               /* Rowan-Robinson & May (2013) */
+  ZL_NARROW_BAND = 7, ZL_BROAD_BAND = 8, ZL_RING_RRM = 9, ZL_FEATURE_RRM = 10
+};
+
+/* Model families: the integrand (zodipy/zodiacal_light_model.py:70-102). */
+enum {
+  ZL_KELSALL = 0, /* (1-A) eps B(T) + A S Phi / R^2, one T_0/delta (brightness.py:21-56) */
+  ZL_RRM = 1      /* B(T) x calibration, T_0/delta per component (brightness.py:59-83) */
+};
 
 /* Arithmetic of the integrand. */
 enum {
@@ -64,15 +76,23 @@ enum {
 
 /* One zodiacal component; geometry derived like zodipy/component.py:39-44. */
 typedef struct ZlComponent {
-  int32_t type;       /* ZL_CLOUD .. ZL_FEATURE */
+  int32_t type;       /* ZL_CLOUD .. ZL_FEATURE_RRM */
   int32_t range;      /* index into ZlModel.cutoff */
   double offset[3];   /* x_0, y_0, z_0 [AU] */
   double sin_i, cos_i, sin_Omega, cos_Omega;
-  double n_0;
-  /* cloud:   alpha, beta, gamma, mu
-   * band:    delta_zeta [rad], v, p, delta_r
-   * ring:    R, sigma_r, sigma_z
-   * feature: R, sigma_r, sigma_z, theta [rad], sigma_theta [rad] */
+  double n_0;         /* unused by fan, comet, interstellar, narrow and broad band */
+  /* own parameters, in the order of the reference's dataclass fields (component.py:47-204):
+   * cloud:        alpha, beta, gamma, mu
+   * band:         delta_zeta [rad], v, p, delta_r
+   * ring:         R, sigma_r, sigma_z
+   * feature:      R, sigma_r, sigma_z, theta [rad], sigma_theta [rad]
+   * fan:          gamma, Z_0, Q, P, R_outer
+   * comet:        gamma, Z_0, P, amp, R_inner, R_outer
+   * interstellar: amp
+   * narrow band:  gamma, A, G, R_inner, R_outer, beta_nb [deg]
+   * broad band:   gamma, A, R_inner, R_outer, beta_bb [deg], sigma_bb [deg]
+   * ring (RRM):   R, sigma_r, sigma_z, A
+   * feature (RRM): R, sigma_r, sigma_z, theta [rad], sigma_theta [rad], A */
   double p[6];
 } ZlComponent;
 
@@ -83,14 +103,21 @@ typedef struct ZlSpectrum {
   double albedo[ZL_MAX_COMPS];
   double C1, C2, C3;           /* phase-function coefficients */
   double solar_irradiance;     /* [MJy/sr] at 1 AU */
+  double calibration;          /* ZL_RRM only: [Jy/cm] (unpack_model.py:121-131); Kelsall ignores it */
   double bb[ZL_MAX_TEMPS];     /* blackbody table [MJy/sr] at ZlModel.temps */
 } ZlSpectrum;
 
-/* A complete Kelsall-type model evaluated at ZL_MAX_SPEC or fewer spectral sets. */
+/* A complete model evaluated at ZL_MAX_SPEC or fewer spectral sets.  For
+ * ZL_KELSALL emissivity/albedo/C1..C3/solar_irradiance apply and T_0/delta are
+ * shared; for ZL_RRM only calibration applies and T_0/delta are per component
+ * (components that share a range must then share T_0 and delta too). */
 typedef struct ZlModel {
   int32_t abi_version;         /* = ZL_ABI_VERSION */
   int32_t n_comps, n_ranges, n_spec, n_nodes, n_temps;
-  double T_0, delta;           /* T(R) = T_0 R^-delta (zodipy/blackbody.py:16-30) */
+  int32_t family;              /* ZL_KELSALL or ZL_RRM */
+  int32_t reserved;
+  double T_0, delta;           /* T(R) = T_0 R^-delta (zodipy/blackbody.py:16-30), ZL_KELSALL */
+  double comp_T_0[ZL_MAX_COMPS], comp_delta[ZL_MAX_COMPS]; /* per component, ZL_RRM */
   double cutoff[ZL_MAX_RANGES][2]; /* inner, outer cutoff radius [AU] (line_of_sight.py:19-26) */
   double temps[ZL_MAX_TEMPS];  /* table temperatures [K], uniformly spaced, increasing */
   double gl_x[ZL_MAX_NODES];   /* Gauss-Legendre nodes on [-1, 1] */
@@ -151,8 +178,8 @@ ZL_API int zl_forward(const ZlModel* model, const double* unit_vectors_dev, int6
  *   d/d T_0, d/d delta
  *   per spectral set s: d/d emissivity[c] (c = 0..n_comps-1), d/d albedo[c],
  *     d/d C1, C2, C3, d/d solar_irradiance (the interpolated scalars)
- * Supported for the built-in component layouts (DIRBE: cloud, 3 bands, ring,
- * feature; Planck: cloud, 3 bands).  The sum over pixels is deterministic:
+ * Supported for ZL_KELSALL models (any mix of the four Kelsall types); a
+ * ZL_RRM model is refused with ZL_ERR_MODEL.  The sum over pixels is deterministic:
  * fixed 128-pixel tiles reduced in a fixed order, independent of the launch. */
 
 /* Number of entries of the gradient vector for this model. */

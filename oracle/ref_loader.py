@@ -26,6 +26,10 @@ import numpy as np
 
 DEFAULT_REF_ROOT = os.environ.get("ZODIPY_REF_ROOT", "/root/reference")
 
+# (1 MJy / AU) in Jy / cm, the unit change astropy applies to the RRM calibration
+# (unpack_model.py:131-132): 1e6 Jy over 1 au = 1.495978707e13 cm (IAU 2012 exact).
+MJY_PER_AU_TO_JY_PER_CM = 1e6 / 1.495978707e13
+
 
 class _Unit:
     def __init__(self, name: str, scale: float = 1.0) -> None:
@@ -177,13 +181,22 @@ def reference_evaluate(
     to the model spectrum's unit; ``weights`` are the already-normalised weights
     (``model.py:94``) or None.
     """
-    import functools
-
     model = ref.model_registry.model_registry.get_model(model_name) if isinstance(model_name, str) else model_name
     spectrum = _V(np.asarray(model.spectrum))
     x = _V(x_in_model_units)
     w = None if weights is None else _V(weights)
     isp = ref.unpack_model.interp_spectral_param
+
+    if type(model).__name__ == "RRM":
+        # unpack_model.py:110-132; the calibration's unit change (MJy/AU -> Jy/cm) is astropy's
+        # and is restated here as a factor
+        comp_params = {label: {"T_0": model.T_0[label], "delta": model.delta[label]} for label in model.comps}
+        cal = isp(x, w, spectrum, model.calibration, bounds_error=bounds_error)
+        shared = {"calibration": float(cal) * MJY_PER_AU_TO_JY_PER_CM}
+        if scalars is not None and "calibration" in scalars:
+            shared["calibration"] = scalars["calibration"]
+        return _run_reference_path(ref, model, unit_vectors, obs_xyz, earth_xyz, bb_table, gauss_quad_degree,
+                                   comp_params, shared)
 
     comp_params = {}
     for label in model.comps:
@@ -214,6 +227,14 @@ def reference_evaluate(
             shared[key] = scalars[key]
         shared["T_0"] = scalars.get("T_0", shared["T_0"])
         shared["delta"] = scalars.get("delta", shared["delta"])
+    return _run_reference_path(ref, model, unit_vectors, obs_xyz, earth_xyz, bb_table, gauss_quad_degree,
+                               comp_params, shared)
+
+
+def _run_reference_path(ref, model, unit_vectors, obs_xyz, earth_xyz, bb_table, gauss_quad_degree, comp_params,
+                        shared):
+    """The reference's ``Model._evaluate`` loop (``model.py:253-277``) with unpacked parameters."""
+    import functools
 
     obs = np.asarray(obs_xyz, dtype=np.float64)
     if obs.ndim == 1:
@@ -268,6 +289,16 @@ def reference_spectral_scalars(ref, model_name, x_in_model_units, weights, bound
         else 0.0
     )
     return out
+
+
+def reference_rrm_calibration(ref, model_name, x_in_model_units, weights, bounds_error=False) -> float:
+    """RRM calibration [Jy/cm] as ``interp_and_unpack_rrm`` forms it (``unpack_model.py:110-132``)."""
+    model = ref.model_registry.model_registry.get_model(model_name)
+    w = None if weights is None else _V(weights)
+    cal = ref.unpack_model.interp_spectral_param(
+        _V(x_in_model_units), w, _V(np.asarray(model.spectrum)), model.calibration, bounds_error=bounds_error
+    )
+    return float(cal) * MJY_PER_AU_TO_JY_PER_CM
 
 
 def reference_fd_gradient(ref, model_name, u, obs, earth, bb_table, x_model, weights, degree, a, rel_step=1e-5):

@@ -183,6 +183,79 @@ def feature_density(X_helio, comp, geom, X_earth):
     return comp["n_0"] * np.exp(-e)
 
 
+def _masked(R, lo, hi):
+    """Radial mask of the RRM densities; outside it the reference leaves zeros (np.zeros_like + filtered fill)."""
+    return np.logical_and(R >= lo, R <= hi)
+
+
+def fan_density(X_helio, comp, geom):
+    """RRM fan (``number_density.py:184-218``)."""
+    _, R, Z = _dist_and_z(X_helio, geom)
+    keep = R <= comp["R_outer"]
+    beta = np.arcsin(Z / R)
+    Z_abs = np.abs(Z)
+    eps = np.where(Z_abs < comp["Z_0"], 2 - (Z_abs / comp["Z_0"]), 1)
+    f = np.cos(beta) ** comp["Q"] * np.exp(-comp["P"] * np.sin(np.abs(beta) ** eps))
+    return np.where(keep, (R ** (-comp["gamma"])) * f, 0.0)
+
+
+def comet_density(X_helio, comp, geom):
+    """RRM comet (``number_density.py:221-256``)."""
+    _, R, Z = _dist_and_z(X_helio, geom)
+    keep = _masked(R, comp["R_inner"], comp["R_outer"])
+    beta = np.arcsin(Z / R)
+    Z_abs = np.abs(Z)
+    eps = np.where(Z_abs < comp["Z_0"], 2 - (Z_abs / comp["Z_0"]), 1)
+    f = np.exp(-comp["P"] * np.sin(np.abs(beta) ** eps))
+    return np.where(keep, comp["amp"] * (R ** (-comp["gamma"])) * f, 0.0)
+
+
+def interstellar_density(X_helio, comp, geom):
+    """RRM interstellar dust (``number_density.py:259-264``): a constant."""
+    return np.full(np.shape(X_helio)[1:], comp["amp"])
+
+
+def narrow_band_density(X_helio, comp, geom):
+    """RRM narrow band (``number_density.py:267-304``)."""
+    _, R, Z = _dist_and_z(X_helio, geom)
+    keep = _masked(R, comp["R_inner"], comp["R_outer"])
+    beta_abs = np.abs(np.rad2deg(np.arcsin(Z / R)))
+    f = np.where(beta_abs < comp["beta_nb"], np.exp(comp["G"] * (beta_abs - comp["beta_nb"])), 0)
+    return np.where(keep, comp["A"] * ((R / comp["R_outer"]) ** (-comp["gamma"])) * f, 0.0)
+
+
+def broad_band_density(X_helio, comp, geom):
+    """RRM broad band (``number_density.py:307-342``)."""
+    _, R, Z = _dist_and_z(X_helio, geom)
+    keep = _masked(R, comp["R_inner"], comp["R_outer"])
+    beta = np.rad2deg(np.arcsin(Z / R))
+    f = np.exp(-0.5 * ((beta - comp["beta_bb"]) / comp["sigma_bb"]) ** 2) + np.exp(
+        -0.5 * ((beta + comp["beta_bb"]) / comp["sigma_bb"]) ** 2
+    )
+    return np.where(keep, comp["A"] * ((R / comp["R_outer"]) ** (-comp["gamma"])) * f, 0.0)
+
+
+def ring_rrm_density(X_helio, comp, geom):
+    """RRM ring: A times the Kelsall ring (``number_density.py:345-370``)."""
+    return comp["A"] * ring_density(X_helio, comp, geom)
+
+
+def feature_rrm_density(X_helio, comp, geom, X_earth):
+    """RRM feature: A times the Kelsall feature (``number_density.py:373-403``)."""
+    return comp["A"] * feature_density(X_helio, comp, geom, X_earth)
+
+
+def rrm_brightness_at_step(r, start, stop, X_obs, u_los, bb_table, density, T_0, delta, calibration):
+    """RRM integrand at one quadrature node (``brightness.py:59-83``)."""
+    R_los = 0.5 * (stop - start) * r + 0.5 * (stop + start)
+    X_los = R_los * u_los
+    X_helio = X_los + X_obs
+    R_helio = np.sqrt(X_helio[0] ** 2 + X_helio[1] ** 2 + X_helio[2] ** 2)
+    temperature = T_0 * R_helio**-delta  # blackbody.py:16-30
+    bb = np.interp(temperature, *bb_table)
+    return bb * density(X_helio) * calibration * 0.5 * (stop - start)
+
+
 def phase_normalization(C1, C2, C3):
     """Analytic phase-function normalisation (``scattering.py:53-59``)."""
     t1 = 2 * np.pi
@@ -225,11 +298,28 @@ def integrate_leggauss(func, points, weights):
     return np.squeeze(sum(func(x) * w for x, w in zip(points, weights)))
 
 
-_DENSITY = {"cloud": cloud_density, "band": band_density, "ring": ring_density, "feature": feature_density}
+_DENSITY = {
+    "cloud": cloud_density,
+    "band": band_density,
+    "ring": ring_density,
+    "feature": feature_density,
+    "fan": fan_density,
+    "comet": comet_density,
+    "interstellar": interstellar_density,
+    "narrow_band": narrow_band_density,
+    "broad_band": broad_band_density,
+    "ring_rrm": ring_rrm_density,
+    "feature_rrm": feature_rrm_density,
+}
+_NEEDS_EARTH = ("feature", "feature_rrm")
 
 
 def comp_type(label: str) -> str:
-    return "band" if label.startswith("band") else label
+    if label.startswith("band"):
+        return "band"
+    if label.endswith("narrow_band"):
+        return "narrow_band"
+    return label
 
 
 def evaluate(desc: dict, unit_vectors, obs_xyz, earth_xyz, fix_b0=False) -> np.ndarray:
@@ -239,7 +329,9 @@ def evaluate(desc: dict, unit_vectors, obs_xyz, earth_xyz, fix_b0=False) -> np.n
     as in ``to_dict()``), ``cutoffs`` {label: (inner, outer)}, ``T_0``,
     ``delta``, ``emissivity`` / ``albedo`` lists, ``C1``..``C3``,
     ``solar_irradiance``, ``bb_table`` (2, n_T) and ``gauss_quad_degree``.
-    ``obs_xyz`` / ``earth_xyz`` are (3,) or (3, N).
+    An RRM model (``family`` = "rrm") has ``T_0`` / ``delta`` as
+    {label: value} and a ``calibration`` [Jy/cm] instead of the Kelsall
+    spectral scalars.  ``obs_xyz`` / ``earth_xyz`` are (3,) or (3, N).
     """
     u = np.asarray(unit_vectors, dtype=np.float64)
     obs = np.asarray(obs_xyz, dtype=np.float64)
@@ -256,10 +348,29 @@ def evaluate(desc: dict, unit_vectors, obs_xyz, earth_xyz, fix_b0=False) -> np.n
         comp = desc["comps"][label]
         geom = component_geometry(comp)
         kind = comp_type(label)
-        if kind == "feature":
-            density = lambda X, c=comp, g=geom: feature_density(X, c, g, earth)  # noqa: E731
+        if kind in _NEEDS_EARTH:
+            density = lambda X, c=comp, g=geom, f=_DENSITY[kind]: f(X, c, g, earth)  # noqa: E731
         else:
             density = lambda X, c=comp, g=geom, f=_DENSITY[kind]: f(X, c, g)  # noqa: E731
+        if desc.get("family") == "rrm":
+            with np.errstate(all="ignore"):
+                out[idx] = integrate_leggauss(
+                    lambda r: rrm_brightness_at_step(
+                        r,
+                        start[label],
+                        stop[label],
+                        obs,
+                        u,
+                        desc["bb_table"],
+                        density,
+                        desc["T_0"][label],
+                        desc["delta"][label],
+                        desc["calibration"],
+                    ),
+                    pts,
+                    wts,
+                )
+            continue
         with np.errstate(all="ignore"):
             out[idx] = integrate_leggauss(
                 lambda r: brightness_at_step(
@@ -301,8 +412,8 @@ def grid_number_density(desc: dict, x, y, z, earth_xyz) -> np.ndarray:
         geom["X_0"] = geom["X_0"].reshape(3, 1, 1, 1)
         kind = comp_type(label)
         with np.errstate(all="ignore"):
-            if kind == "feature":
-                out[idx] = feature_density(grid, comp, geom, earth)
+            if kind in _NEEDS_EARTH:
+                out[idx] = _DENSITY[kind](grid, comp, geom, earth)
             else:
                 out[idx] = _DENSITY[kind](grid, comp, geom)
     return out

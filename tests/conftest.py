@@ -36,6 +36,18 @@ def oracle_desc(case, models=None):
     name = str(case["model"])
     m = models[name]
     labels = list(m["comps"])
+    if m.get("family") == "rrm":
+        return {
+            "family": "rrm",
+            "labels": labels,
+            "comps": m["comps"],
+            "cutoffs": {k: tuple(v) for k, v in m["cutoffs"].items()},
+            "T_0": m["T_0"],
+            "delta": m["delta"],
+            "calibration": float(case["calibration"]),
+            "bb_table": case["bb_table"],
+            "gauss_quad_degree": int(case["degree"]),
+        }
     return {
         "labels": labels,
         "comps": m["comps"],

@@ -18,7 +18,8 @@ those inputs to the per-component emission.  Outputs:
                       points (tests/dirbe_tabulated.py of the reference)
   grid_<case>.npz     inputs + reference grid_number_density output
 
-``python tests/golden/make_golden.py grid`` regenerates only the grid fixtures.
+``python tests/golden/make_golden.py grid`` regenerates only the grid fixtures,
+``... rrm`` only ref_models.json and the RRM fixtures.
 """
 
 from __future__ import annotations
@@ -40,6 +41,7 @@ from oracle.ref_loader import (  # noqa: E402
     load_reference,
     reference_evaluate,
     reference_fd_gradient,
+    reference_rrm_calibration,
     reference_spectral_scalars,
 )
 from zodipy_gb300.ephemeris import earth_position, iso_to_mjd  # noqa: E402
@@ -53,12 +55,25 @@ def dump_models(ref) -> dict:
     reg = ref.model_registry.model_registry
     for name in reg.models:
         m = reg.get_model(name)
-        if type(m).__name__ != "Kelsall":
-            continue
         d = m.to_dict()
 
         def seq(v):
             return None if v is None else [float(x) for x in v]
+
+        cutoffs = {lbl.value: [float(v) for v in ref.line_of_sight.COMPONENT_CUTOFFS[lbl]] for lbl in m.comps}
+        comps = {k: {kk: float(vv) for kk, vv in v.items()} for k, v in d["comps"].items()}
+        if type(m).__name__ == "RRM":
+            out[name] = {
+                "family": "rrm",
+                "comps": comps,
+                "spectrum": seq(np.asarray(m.spectrum)),
+                "spectrum_unit": "micron",
+                "T_0": {k: float(v) for k, v in d["T_0"].items()},
+                "delta": {k: float(v) for k, v in d["delta"].items()},
+                "calibration": seq(d["calibration"]),
+                "cutoffs": cutoffs,
+            }
+            continue
 
         out[name] = {
             "comps": {k: {kk: float(vv) for kk, vv in v.items()} for k, v in d["comps"].items()},
@@ -72,15 +87,13 @@ def dump_models(ref) -> dict:
             "C1": seq(d["C1"]),
             "C2": seq(d["C2"]),
             "C3": seq(d["C3"]),
-            "cutoffs": {
-                lbl.value: [float(v) for v in ref.line_of_sight.COMPONENT_CUTOFFS[lbl]] for lbl in m.comps
-            },
+            "cutoffs": cutoffs,
         }
     return out
 
 
 def model_unit(name: str) -> str:
-    return "micron" if name == "dirbe" else "GHz"
+    return "micron" if name in ("dirbe", "rrm-experimental") else "GHz"
 
 
 def to_model_units(x, user_unit: str, name: str) -> np.ndarray:
@@ -99,7 +112,12 @@ def make_case(ref, name, x, user_unit, weights, u, obs, earth, degree):
     bb = zodi_oracle.planck_table(x, w_norm, unit=user_unit)
     xm = to_model_units(x, user_unit, name)
     out = reference_evaluate(ref, name, u, obs, earth, bb, xm, w_norm, degree, bounds_error=False)
-    scal = reference_spectral_scalars(ref, name, xm, w_norm, bounds_error=False)
+    if name.startswith("rrm"):
+        scal = {"emissivity": [], "albedo": [], "C1": 0.0, "C2": 0.0, "C3": 0.0, "solar_irradiance": 0.0}
+        scal["calibration"] = reference_rrm_calibration(ref, name, xm, w_norm)
+    else:
+        scal = reference_spectral_scalars(ref, name, xm, w_norm, bounds_error=False)
+        scal["calibration"] = 0.0
     return dict(
         model=np.array(name),
         x=np.atleast_1d(np.asarray(x, dtype=np.float64)),
@@ -114,6 +132,7 @@ def make_case(ref, name, x, user_unit, weights, u, obs, earth, degree):
         emissivity=np.array(scal["emissivity"]),
         albedo=np.array(scal["albedo"]),
         C=np.array([scal["C1"], scal["C2"], scal["C3"], scal["solar_irradiance"]]),
+        calibration=np.array(scal["calibration"]),
         ref_out=out,
     )
 
@@ -164,6 +183,50 @@ def make_grids(ref) -> None:
         nd.get_earthpos_inst = saved
 
 
+def make_rrm(ref) -> None:
+    """Rowan-Robinson & May model: line-of-sight cases and density grids."""
+    earth_2022 = earth_position(iso_to_mjd("2022-01-01T00:00:00"))
+    earth_1990 = earth_position(iso_to_mjd("1990-06-11T00:00:00"))
+    dirs_rand = random_sphere(256, seed=17)
+    lam = np.linspace(10.0, 14.0, 16)
+    cases = {
+        # observer at 1 AU: inside every inner cutoff
+        "rrm25_nside8": ("rrm-experimental", 25.0, None, pix2vec_ring(8), [0.9833, 0.0, 0.0], earth_2022, 50),
+        # just outside Mars's orbit: the fan's outer and the bands' and comet's inner cutoffs collapse to eps
+        "rrm60_mars": ("rrm-experimental", 60.0, None, dirs_rand, [1.2, -1.05, 0.02], earth_2022, 50),
+        # beyond the asteroid belt: the bands' both cutoffs collapse
+        "rrm100_belt": ("rrm-experimental", 100.0, None, dirs_rand, [2.5, 2.6, 0.1], earth_2022, 50),
+        "rrm12_bandpass": ("rrm-experimental", lam, np.exp(-0.5 * ((lam - 12.0) / 1.0) ** 2), dirs_rand,
+                           [0.2, 0.99, 0.0], earth_1990, 100),
+    }
+    for key, (name, x, w, u, obs, earth, deg) in cases.items():
+        payload = make_case(ref, name, x, "micron", w, u, np.asarray(obs, dtype=np.float64), earth, deg)
+        np.savez_compressed(os.path.join(HERE, f"los_{key}.npz"), **payload)
+    nd = ref.number_density
+    grid_cases = {
+        "rrm_wide": (np.linspace(0, 5, 10), np.linspace(0, 5, 10), np.linspace(0, 2, 6), "2022-01-01T00:00:00"),
+        "rrm_inner": (np.linspace(-2, 2, 21), np.linspace(-2, 2, 17), np.linspace(-0.3, 0.3, 7), "2022-06-01T00:00:00"),
+    }
+    saved = nd.get_earthpos_inst
+    try:
+        for key, (x, y, z, iso) in grid_cases.items():
+            earth = earth_position(iso_to_mjd(iso)).reshape(3)
+            nd.get_earthpos_inst = lambda obstime, ephemeris, e=earth: e.copy()
+            out = nd.grid_number_density(x, y, z, obstime=None, model="rrm-experimental")
+            np.savez_compressed(
+                os.path.join(HERE, f"grid_{key}.npz"),
+                model=np.array("rrm-experimental"),
+                x=x,
+                y=y,
+                z=z,
+                obstime=np.array(iso),
+                earth=earth,
+                ref_out=np.asarray(out, dtype=np.float64),
+            )
+    finally:
+        nd.get_earthpos_inst = saved
+
+
 def main() -> None:
     ref_root = os.environ.get("ZODIPY_REF_ROOT", DEFAULT_REF_ROOT)
     ref = load_reference(ref_root)
@@ -171,7 +234,14 @@ def main() -> None:
         make_grids(ref)
         print("wrote grid fixtures to", HERE)
         return
+    if sys.argv[1:] == ["rrm"]:
+        with open(os.path.join(HERE, "ref_models.json"), "w") as f:
+            json.dump(dump_models(ref), f, indent=1)
+        make_rrm(ref)
+        print("wrote RRM fixtures to", HERE)
+        return
     make_grids(ref)
+    make_rrm(ref)
     models = dump_models(ref)
     with open(os.path.join(HERE, "ref_models.json"), "w") as f:
         json.dump(models, f, indent=1)

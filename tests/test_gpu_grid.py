@@ -23,7 +23,7 @@ from conftest import GOLDEN, cuda_ok, ref_models
 pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not cuda_ok(), reason="needs CUDA")]
 
 RTOL, ATOL = 1e-11, 1e-300
-GRID_CASES = ["dirbe_wide", "dirbe_near_earth", "planck13_wide", "planck18_ring"]
+GRID_CASES = ["dirbe_wide", "dirbe_near_earth", "planck13_wide", "planck18_ring", "rrm_wide", "rrm_inner"]
 
 
 def _band_condition(name, x, y, z):

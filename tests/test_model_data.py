@@ -16,6 +16,12 @@ def test_parameter_data_equals_reference_registry():
         m = model_registry.get_model(name)
         d = m.to_dict()
         assert d["comps"] == rec["comps"], name
+        assert list(d["comps"]) == list(rec["comps"]), name  # component (output) order
+        if rec.get("family") == "rrm":
+            assert d["T_0"] == rec["T_0"] and d["delta"] == rec["delta"]
+            assert list(d["calibration"]) == rec["calibration"]
+            assert list(np.asarray(m.spectrum.value)) == rec["spectrum"]
+            continue
         assert d["T_0"] == rec["T_0"] and d["delta"] == rec["delta"]
         assert list(np.asarray(m.spectrum.value)) == rec["spectrum"]
         assert {k: list(v) for k, v in d["emissivities"].items()} == rec["emissivities"]
@@ -153,3 +159,39 @@ def test_parameter_vector_round_trip():
     names = params.names(m.zl_model, m.comp_labels)
     assert names[:6] == ["comps.cloud.x_0", "comps.cloud.y_0", "comps.cloud.z_0", "comps.cloud.i", "comps.cloud.Omega", "comps.cloud.n_0"]
     assert names[-4:] == ["C1", "C2", "C3", "solar_irradiance"]
+
+
+def test_rrm_calibration_unpacking():
+    """unpack_model.py:110-132: calibration interpolated over the IRAS bands, in Jy/cm."""
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import units as u
+
+    for key in ("rrm25_nside8", "rrm12_bandpass"):
+        z = np.load(f"{GOLDEN}/los_{key}.npz")
+        x = z["x"] * u.micron if not bool(z["x_is_scalar"]) else float(z["x"][0]) * u.micron
+        w = None if bool(z["x_is_scalar"]) else z["weights"]
+        m = zg.Model(x, weights=w, name="rrm-experimental", extrapolate=True, gauss_quad_degree=int(z["degree"]))
+        zl = m.zl_model
+        assert zl.family == 1
+        np.testing.assert_allclose(zl.spec[0].calibration, float(z["calibration"]), rtol=1e-15)
+        assert [zl.comp_T_0[c] for c in range(zl.n_comps)] == [255.0] * 5 + [305.0] + [255.0] * 2
+        np.testing.assert_allclose(m._b_nu_table, z["bb_table"], rtol=1e-13)
+
+
+def test_rrm_parameters_round_trip_and_adjoint_refusal(lib):
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import _lib, engine
+    from zodipy_gb300 import units as u
+
+    m = zg.Model(25 * u.micron, name="rrm-experimental")
+    p = m.get_parameters()
+    assert list(p) == ["comps", "spectrum", "T_0", "delta", "calibration"]
+    p2 = {**p, "T_0": {**p["T_0"], "fan": 260.0}}
+    p2["comps"] = {**p["comps"], "fan": {**p["comps"]["fan"], "Q": 11.0}}
+    m.update_parameters(p2)
+    assert m.get_parameters()["T_0"]["fan"] == 260.0 and m.get_parameters()["comps"]["fan"]["Q"] == 11.0
+    assert m.zl_model.comp_T_0[0] == 260.0 and m.zl_model.comp[0].p[2] == 11.0
+    # the fan no longer shares its temperature law with anything, and the bands still share one range
+    assert m.zl_model.comp[2].range == m.zl_model.comp[3].range == m.zl_model.comp[4].range
+    with pytest.raises(_lib.ZodiGBError, match="Kelsall"):
+        engine.grad_count(m.zl_model)

@@ -63,7 +63,7 @@ def test_oracle_chunked_is_partition_independent():
     np.testing.assert_array_equal(whole, parts)
 
 
-GRID_CASES = ["dirbe_wide", "dirbe_near_earth", "planck13_wide", "planck18_ring"]
+GRID_CASES = ["dirbe_wide", "dirbe_near_earth", "planck13_wide", "planck18_ring", "rrm_wide", "rrm_inner"]
 
 
 def grid_desc(name):

@@ -12,7 +12,7 @@ import os
 
 from ._build import LIB_PATH
 
-ZL_ABI_VERSION = 1
+ZL_ABI_VERSION = 2
 ZL_MAX_COMPS = 8
 ZL_MAX_RANGES = 8
 ZL_MAX_SPEC = 4
@@ -20,6 +20,8 @@ ZL_MAX_NODES = 128
 ZL_MAX_TEMPS = 128
 
 ZL_CLOUD, ZL_BAND, ZL_RING, ZL_FEATURE = 0, 1, 2, 3
+ZL_FAN, ZL_COMET, ZL_INTERSTELLAR, ZL_NARROW_BAND, ZL_BROAD_BAND, ZL_RING_RRM, ZL_FEATURE_RRM = 4, 5, 6, 7, 8, 9, 10
+ZL_KELSALL, ZL_RRM = 0, 1
 ZL_PREC_F64, ZL_PREC_F32 = 0, 1
 ZL_OK, ZL_ERR_ARG, ZL_ERR_CUDA, ZL_ERR_MODEL, ZL_ERR_SPACE = 0, -1, -2, -3, -4
 
@@ -48,6 +50,7 @@ class ZlSpectrum(ctypes.Structure):
         ("C2", ctypes.c_double),
         ("C3", ctypes.c_double),
         ("solar_irradiance", ctypes.c_double),
+        ("calibration", ctypes.c_double),
         ("bb", ctypes.c_double * ZL_MAX_TEMPS),
     ]
 
@@ -60,8 +63,12 @@ class ZlModel(ctypes.Structure):
         ("n_spec", ctypes.c_int32),
         ("n_nodes", ctypes.c_int32),
         ("n_temps", ctypes.c_int32),
+        ("family", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("T_0", ctypes.c_double),
         ("delta", ctypes.c_double),
+        ("comp_T_0", ctypes.c_double * ZL_MAX_COMPS),
+        ("comp_delta", ctypes.c_double * ZL_MAX_COMPS),
         ("cutoff", (ctypes.c_double * 2) * ZL_MAX_RANGES),
         ("temps", ctypes.c_double * ZL_MAX_TEMPS),
         ("gl_x", ctypes.c_double * ZL_MAX_NODES),

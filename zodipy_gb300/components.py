@@ -1,8 +1,8 @@
-"""Zodiacal dust components of the Kelsall et al. (1998) model family.
+"""Zodiacal dust components of the Kelsall et al. (1998) and Rowan-Robinson & May (2013) models.
 
 The field names and their order are part of the public parameter-dict format
 (``Model.get_parameters`` / ``update_parameters``), so they match
-``zodipy/component.py:14-136`` of the reference.  Derived geometry (the
+``zodipy/component.py:14-223`` of the reference.  Derived geometry (the
 offset vector, sin/cos of inclination and ascending node, angles in radians)
 is computed once per component like ``component.py:39-44,87-89,133-136`` and
 packed into the kernel parameter block by ``zodipy_gb300.packing``.
@@ -16,7 +16,7 @@ from enum import Enum
 
 
 class ComponentLabel(Enum):
-    """Component labels (``component.py:207-223``; RRM labels are not modelled here)."""
+    """Component labels (``component.py:207-223``)."""
 
     CLOUD = "cloud"
     BAND1 = "band1"
@@ -24,6 +24,14 @@ class ComponentLabel(Enum):
     BAND3 = "band3"
     RING = "ring"
     FEATURE = "feature"
+    FAN = "fan"
+    COMET = "comet"
+    INTERSTELLAR = "interstellar"
+    INNER_NARROW_BAND = "inner_narrow_band"
+    OUTER_NARROW_BAND = "outer_narrow_band"
+    BROAD_BAND = "broad_band"
+    RING_RRM = "ring_rrm"
+    FEATURE_RRM = "feature_rrm"
 
 
 @dataclass
@@ -112,5 +120,85 @@ class Feature(ZodiacalComponent):
         self.sigma_theta_rad = math.radians(self.sigma_theta)
 
 
+@dataclass
+class Fan(ZodiacalComponent):
+    """RRM fan: radial power law gamma, vertical shape Z_0, Q, P, inside R_outer (RRM eq. 3)."""
+
+    gamma: float
+    Z_0: float
+    Q: float
+    P: float
+    R_outer: float
+
+
+@dataclass
+class Comet(ZodiacalComponent):
+    """RRM cometary dust between R_inner and R_outer."""
+
+    gamma: float
+    Z_0: float
+    P: float
+    amp: float
+    R_inner: float
+    R_outer: float
+
+
+@dataclass
+class Interstellar(ZodiacalComponent):
+    """RRM interstellar dust: a constant density amp."""
+
+    amp: float
+
+
+@dataclass
+class NarrowBand(ZodiacalComponent):
+    """RRM narrow asteroidal band: latitude cut beta_nb [deg] with fall-off G (RRM eq. 4)."""
+
+    gamma: float
+    A: float
+    G: float
+    R_inner: float
+    R_outer: float
+    beta_nb: float
+
+
+@dataclass
+class BroadBand(ZodiacalComponent):
+    """RRM broad asteroidal band: Gaussians at +-beta_bb [deg] of width sigma_bb (RRM eq. 5)."""
+
+    gamma: float
+    A: float
+    R_inner: float
+    R_outer: float
+    beta_bb: float
+    sigma_bb: float
+
+
+@dataclass
+class RingRRM(Ring):
+    """RRM circumsolar ring: the Kelsall ring scaled by A."""
+
+    A: float
+
+
+@dataclass
+class FeatureRRM(Feature):
+    """RRM Earth-trailing feature: the Kelsall feature scaled by A."""
+
+    A: float
+
+
 # Numeric component type codes shared with the CUDA kernels (include/zodigb.h).
-COMPONENT_TYPE_CODE = {Cloud: 0, Band: 1, Ring: 2, Feature: 3}
+COMPONENT_TYPE_CODE = {
+    Cloud: 0,
+    Band: 1,
+    Ring: 2,
+    Feature: 3,
+    Fan: 4,
+    Comet: 5,
+    Interstellar: 6,
+    NarrowBand: 7,
+    BroadBand: 8,
+    RingRRM: 9,
+    FeatureRRM: 10,
+}

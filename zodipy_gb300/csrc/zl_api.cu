@@ -115,10 +115,15 @@ extern "C" ZL_API int zl_model_check(const ZlModel* m) {
   for (int t = 0; t < m->n_temps; ++t)
     if (std::fabs(m->temps[t] - (m->temps[0] + t * dt)) > 1e-9 * std::fabs(m->temps[m->n_temps - 1]))
       return fail(ZL_ERR_MODEL, "temps must be uniformly spaced (index %d)", t);
+  if (m->family != ZL_KELSALL && m->family != ZL_RRM) return fail(ZL_ERR_MODEL, "bad model family %d", m->family);
   for (int c = 0; c < m->n_comps; ++c) {
     const ZlComponent& C = m->comp[c];
-    if (C.type < ZL_CLOUD || C.type > ZL_FEATURE) return fail(ZL_ERR_MODEL, "component %d: bad type %d", c, C.type);
+    if (C.type < ZL_CLOUD || C.type > ZL_FEATURE_RRM) return fail(ZL_ERR_MODEL, "component %d: bad type %d", c, C.type);
     if (C.range < 0 || C.range >= m->n_ranges) return fail(ZL_ERR_MODEL, "component %d: range %d out of [0,%d)", c, C.range, m->n_ranges);
+    if (m->family == ZL_RRM)
+      for (int j = 0; j < c; ++j)
+        if (m->comp[j].range == C.range && (m->comp_T_0[j] != m->comp_T_0[c] || m->comp_delta[j] != m->comp_delta[c]))
+          return fail(ZL_ERR_MODEL, "components %d and %d share range %d but not T_0/delta", j, c, C.range);
   }
   for (int r = 0; r < m->n_ranges; ++r)
     if (!(m->cutoff[r][0] >= 0.0) || !is_finite(m->cutoff[r][1]) || !(m->cutoff[r][1] > 0.0))
@@ -165,7 +170,9 @@ void first_in_range(const ZlModel& m, int32_t* out) {
 }
 
 // 1 = DIRBE-like (cloud | 3 bands on one range | ring | feature), 2 = Planck-like, 0 = generic
+// (every RRM model runs the generic layout)
 int detect_layout(const ZlModel& m) {
+  if (m.family != ZL_KELSALL) return 0;
   int32_t first[ZL_MAX_COMPS];
   first_in_range(m, first);
   static const int dirbe_t[6] = {ZL_CLOUD, ZL_BAND, ZL_BAND, ZL_BAND, ZL_RING, ZL_FEATURE};
@@ -198,9 +205,14 @@ void build_f64(const ZlModel& m, KParamsF64* P) {
     P->phase_norm[s] = 1 / (t1 * (t2 + t3 + t4));
   }
   first_in_range(m, P->first_in_range);
-  for (int c = 0; c < m.n_comps; ++c)
-    for (int s = 0; s < m.n_spec; ++s)
-      if (m.spec[s].albedo[c] != 0.0) P->range_scat[m.comp[c].range] = 1;
+  for (int c = 0; c < m.n_comps; ++c) {
+    const int r = m.comp[c].range;
+    P->range_T0[r] = m.family == ZL_RRM ? m.comp_T_0[c] : m.T_0;
+    P->range_delta[r] = m.family == ZL_RRM ? m.comp_delta[c] : m.delta;
+    if (m.family == ZL_KELSALL)
+      for (int s = 0; s < m.n_spec; ++s)
+        if (m.spec[s].albedo[c] != 0.0) P->range_scat[r] = 1;
+  }
 }
 
 void build_f32(const ZlModel& m, KParamsF32* P) {
@@ -236,6 +248,8 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
     K.first_in_range = first[c];
     K.zero_offset = (C.offset[0] == 0.0 && C.offset[1] == 0.0 && C.offset[2] == 0.0) ? 1 : 0;
     K.share_t4 = -1;
+    K.T0 = (float)(m.family == ZL_RRM ? m.comp_T_0[c] : m.T_0);
+    K.neg_delta = (float)(-(m.family == ZL_RRM ? m.comp_delta[c] : m.delta));
     if (C.type == ZL_BAND)
       for (int j = 0; j < c; ++j) {
         const ZlComponent& Cj = m.comp[j];
@@ -272,15 +286,58 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
         break;
       case ZL_RING:
       case ZL_FEATURE:
-        K.c[0] = (float)C.n_0;
+      case ZL_RING_RRM:
+      case ZL_FEATURE_RRM:
+        K.c[0] = (float)(C.type == ZL_RING_RRM ? p[3] * C.n_0 : C.type == ZL_FEATURE_RRM ? p[5] * C.n_0 : C.n_0);
         K.c[1] = (float)p[0];
         K.c[2] = (float)(L2E / (p[1] * p[1]));
         K.c[3] = (float)(L2E / p[2]);
         split(p[0] * p[0], &K.c[4], &K.c[5]);
-        if (C.type == ZL_FEATURE) {
+        if (featurelike(C.type)) {
           K.c[6] = (float)p[3];
           K.c[7] = (float)(L2E / (p[4] * p[4]));
         }
+        break;
+      case ZL_INTERSTELLAR:
+        K.c[0] = (float)p[0];
+        break;
+      case ZL_FAN:  // gamma, Z_0, Q, P, R_outer
+        K.c[0] = 1.0f;
+        K.c[1] = (float)(-p[0]);
+        K.c[2] = (float)(0.5 * p[2]);
+        K.c[3] = (float)(-p[3] * L2E);
+        K.c[4] = (float)(1.0 / p[1]);
+        split(p[4] * p[4], &K.c[10], &K.c[11]);
+        break;
+      case ZL_COMET:  // gamma, Z_0, P, amp, R_inner, R_outer
+        K.c[0] = (float)p[3];
+        K.c[1] = (float)(-p[0]);
+        K.c[3] = (float)(-p[2] * L2E);
+        K.c[4] = (float)(1.0 / p[1]);
+        split(p[4] * p[4], &K.c[8], &K.c[9]);
+        split(p[5] * p[5], &K.c[10], &K.c[11]);
+        break;
+      case ZL_NARROW_BAND: {  // gamma, A, G, R_inner, R_outer, beta_nb [deg]
+        K.c[0] = (float)p[1];
+        K.c[1] = (float)(-p[0]);
+        K.c[2] = (float)(p[2] * L2E);
+        K.c[3] = (float)p[5];
+        K.c[5] = (float)(p[0] * std::log2(p[4]));
+        // |beta| < beta_nb  <=>  (Z/R)^2 < sin^2(beta_nb) for beta_nb in (0, 90]
+        const double sb = p[5] <= 0.0 ? 0.0 : (p[5] >= 90.0 ? 1.0 : std::sin(p[5] * (M_PI / 180.0)));
+        split(sb * sb, &K.c[6], &K.c[7]);
+        split(p[3] * p[3], &K.c[8], &K.c[9]);
+        split(p[4] * p[4], &K.c[10], &K.c[11]);
+        break;
+      }
+      case ZL_BROAD_BAND:  // gamma, A, R_inner, R_outer, beta_bb [deg], sigma_bb [deg]
+        K.c[0] = (float)p[1];
+        K.c[1] = (float)(-p[0]);
+        K.c[2] = (float)p[4];
+        K.c[3] = (float)(1.0 / p[5]);
+        K.c[5] = (float)(p[0] * std::log2(p[3]));
+        split(p[2] * p[2], &K.c[8], &K.c[9]);
+        split(p[3] * p[3], &K.c[10], &K.c[11]);
         break;
     }
   }
@@ -288,6 +345,11 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
     const ZlSpectrum& S = m.spec[s];
     KSpecF32& K = P->spec[s];
     for (int c = 0; c < m.n_comps; ++c) {
+      if (m.family == ZL_RRM) {  // brightness.py:83: B(T) n calibration
+        K.em1[c] = (float)S.calibration;
+        K.alb[c] = 0.f;
+        continue;
+      }
       K.em1[c] = (float)((1.0 - S.albedo[c]) * S.emissivity[c]);
       K.alb[c] = (float)S.albedo[c];
       if (S.albedo[c] != 0.0) P->has_scat = 1;
@@ -360,6 +422,7 @@ constexpr int kBwdTile = 128;
 int64_t bwd_tiles(int64_t n_pix) { return (n_pix + kBwdTile - 1) / kBwdTile; }
 
 int bwd_layout(const ZlModel& m, int* layout) {
+  if (m.family != ZL_KELSALL) return fail(ZL_ERR_MODEL, "the adjoint supports Kelsall models only (this is an RRM model)");
   const int l = detect_layout(m);
   if (l == 0)
     return fail(ZL_ERR_MODEL,

@@ -33,13 +33,25 @@ struct KParamsF64 {
   double phase_norm[ZL_MAX_SPEC];           // scattering.py:53-59
   int32_t first_in_range[ZL_MAX_COMPS];     // component starts a new LOS range group
   int32_t range_scat[ZL_MAX_RANGES];        // some component of the range has albedo != 0
+  double range_T0[ZL_MAX_RANGES], range_delta[ZL_MAX_RANGES];  // T = T_0 R^-delta of the range's components
 };
 
-// Per-component constants of the float32 kernel (Kelsall-98 densities).
+// Component-type predicates shared by the kernels.
+__host__ __device__ constexpr bool ringlike(int t) {
+  return t == ZL_RING || t == ZL_FEATURE || t == ZL_RING_RRM || t == ZL_FEATURE_RRM;
+}
+__host__ __device__ constexpr bool featurelike(int t) { return t == ZL_FEATURE || t == ZL_FEATURE_RRM; }
+// RRM densities that are zero outside [R_inner, R_outer] (number_density.py:184-342)
+__host__ __device__ constexpr bool masked(int t) {
+  return t == ZL_FAN || t == ZL_COMET || t == ZL_NARROW_BAND || t == ZL_BROAD_BAND;
+}
+
+// Per-component constants of the float32 kernel.
 struct KCompF32 {
   int32_t type, range, first_in_range, zero_offset;
   int32_t share_t4;  // band: index of an earlier band with the same delta_r (reuse its 1 - e^-y), else -1
-  int32_t pad_i[3];
+  int32_t pad_i;
+  float T0, neg_delta;     // T = T_0 R^-delta of this component's range (generic layout)
   float nx, ny, nz;        // unit normal of the symmetry plane (sinO sini, -cosO sini, cosi)
   float nx_lo, ny_lo, nz_lo;  // low parts of the normal for float-float heights
   float ox, oy, oz;        // offset X_0 [AU]
@@ -50,7 +62,15 @@ struct KCompF32 {
   //  ring:    c0=n_0, c1=R, c2=log2(e)/sigma_r^2, c3=log2(e)/sigma_z, c4=R^2 (hi), c5=R^2 (lo)
   //  feature: c0=n_0, c1=R, c2=log2(e)/sigma_r^2, c3=log2(e)/sigma_z, c4=R^2 (hi), c5=R^2 (lo),
   //           c6=theta_rad, c7=log2(e)/sigma_theta_rad^2
-  float c[8];
+  //  RRM ring / feature: as ring / feature with c0 = A n_0
+  //  fan:     c1=-gamma, c2=Q/2, c3=-P log2(e), c4=1/Z_0
+  //  comet:   c0=amp, c1=-gamma, c3=-P log2(e), c4=1/Z_0
+  //  interstellar: c0=amp
+  //  narrow band: c0=A, c1=-gamma, c2=G log2(e), c3=beta_nb [deg], c5=gamma log2(R_outer),
+  //           c6,c7=sin^2(beta_nb) (hi, lo)
+  //  broad band:  c0=A, c1=-gamma, c2=beta_bb [deg], c3=1/sigma_bb, c5=gamma log2(R_outer)
+  //  masked RRM types: c8,c9 = R_inner^2 (hi, lo), c10,c11 = R_outer^2 (hi, lo)
+  float c[12];
 };
 
 struct KSpecF32 {

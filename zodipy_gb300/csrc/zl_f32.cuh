@@ -96,4 +96,45 @@ __device__ __forceinline__ float sq_plus_ff(ff w, ff c) {
   return fmaf(w.hi, w.hi, c.hi) + fmaf(2.f * w.hi, w.lo, c.lo);
 }
 
+// w^2 + c as a float-float (exact square of w.hi, first-order low parts)
+__device__ __forceinline__ ff sq_plus_ff2(ff w, ff c) {
+  const float p = w.hi * w.hi;
+  const float pe = fmaf(w.hi, w.hi, -p);
+  const ff s = ff_two_sum(p, c.hi);
+  return ff_quick(s.hi, s.lo + (pe + fmaf(2.f * w.hi, w.lo, c.lo)));
+}
+
+// a < b for normalised float-float values
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+
+// Fan, comet, narrow and broad band of the RRM model (number_density.py:184-342) in float32.
+// The radial mask R_inner <= |X - X_0| <= R_outer and the narrow band's cut |beta| < beta_nb are
+// decided on float-float squares (|X - X_0|^2 = w^2 + b^2, Z^2 < sin^2(beta_nb) R^2), so float32
+// rounding cannot move a node across them; the values inside are plain float32.
+// (hs, x, wm, b2): the distance terms of the node; (z1, z0): Z = z1 x + z0; Z, rinv, lg2R: float32
+// height above the symmetry plane, 1/R and log2 R of the same node.
+__device__ __forceinline__ float rrm_masked_density(const KCompF32& C, int type, ff hs, ff x, ff wm, ff b2, ff z1,
+                                                    ff z0, float Z, float rinv, float lg2R) {
+  const ff R2 = sq_plus_ff2(lin_ff2(hs, x, wm), b2);
+  if (ff_lt(R2, ff{C.c[8], C.c[9]}) || ff_lt(ff{C.c[10], C.c[11]}, R2)) return 0.f;
+  const float s = fminf(fmaxf(Z * rinv, -1.f), 1.f);  // sin(beta)
+  const float beta = asinf(s);
+  if (type == ZL_FAN || type == ZL_COMET) {
+    const float za = fabsf(Z) * C.c[4];  // |Z| / Z_0
+    const float eps = za < 1.f ? 2.f - za : 1.f;
+    float f = ex2_ftz(C.c[3] * sinf(ex2_ftz(eps * lg2_ftz(fabsf(beta)))));  // exp(-P sin(|beta|^eps))
+    if (type == ZL_FAN && C.c[2] != 0.f) f *= ex2_ftz(C.c[2] * lg2_ftz(fmaxf(1.f - s * s, 0.f)));  // cos^Q
+    return C.c[0] * ex2_ftz(C.c[1] * lg2R) * f;
+  }
+  const float bdeg = beta * 57.29577951308232f;
+  const float radial = ex2_ftz(fmaf(C.c[1], lg2R, C.c[5]));  // (R / R_outer)^-gamma
+  if (type == ZL_NARROW_BAND) {
+    const ff Zf = lin_ff2(z1, x, z0);
+    if (!ff_lt(ff_mul(Zf, Zf), ff_mul(ff{C.c[6], C.c[7]}, R2))) return 0.f;
+    return C.c[0] * radial * ex2_ftz(C.c[2] * (fabsf(bdeg) - C.c[3]));
+  }
+  const float a = (bdeg - C.c[2]) * C.c[3], b = (bdeg + C.c[2]) * C.c[3];
+  return C.c[0] * radial * (ex2_ftz(-0.5f * kLog2e * (a * a)) + ex2_ftz(-0.5f * kLog2e * (b * b)));
+}
+
 }  // namespace zl

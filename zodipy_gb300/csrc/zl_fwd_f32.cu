@@ -1,4 +1,6 @@
-// Fast forward kernel: the Kelsall integrand in float32 on the FP32/MUFU pipes.
+// Fast forward kernel: the line-of-sight integrand in float32 on the FP32/MUFU pipes
+// (Kelsall, zodipy/brightness.py:21-56; RRM, zodipy/brightness.py:59-83, through the
+// generic layout).
 //
 // Same integral as the float64 kernel (zodipy/model.py:253-277); what changes is
 // the arithmetic, chosen for GB300 where FP64 runs at a small fraction of FP32:
@@ -115,16 +117,16 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       wm_c[c] = mh_c[c];
       b2_c[c] = b2h;
       cw_c[c] = ff{0.f, 0.f};
-      if (!C.zero_offset || (PRECISE && (type == ZL_RING || type == ZL_FEATURE))) {
+      if (!C.zero_offset || (PRECISE && ringlike(type)) || masked(type)) {
         const ff beta = C.zero_offset ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
         const ff d2 = C.zero_offset ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
         const ff bb = ff_add(d2, ff_neg(ff_mul(beta, beta)));
         wm_c[c] = ff_add(md, beta);
         b2_c[c] = fmaxf(bb.hi + bb.lo, 0.f);
-        cw_c[c] = ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
+        cw_c[c] = masked(type) ? bb : ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
       }
       fx1[c] = fx0[c] = fy1[c] = fy0[c] = 0.f;
-      if (type == ZL_FEATURE) {
+      if (featurelike(type)) {
         // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
         // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
         // two coordinates that are linear in the node abscissa
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
         const KCompF32& C = P.comp[c];
         const int type = L::generic ? C.type : L::type(c);
         const bool first = L::generic ? (C.first_in_range != 0) : L::first(c);
-        const bool precise = PRECISE && (type == ZL_RING || type == ZL_FEATURE);
+        const bool precise = PRECISE && ringlike(type);
         if (first) {
           // brightness.py:27-33 — heliocentric distance of the node, R^2 = w^2 + b^2, and temperature
           wh = lin_ff(hs_c[c], xk, mh_c[c]);
@@ -178,10 +180,10 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           rinv = rsqrt_ftz(R2);
           // one Newton step where 1/R feeds the bands' e^-(zeta/dzeta)^6 (sensitivity 6 x^6);
           // the ring/feature distance is corrected from R^2 - R0^2 below instead
-          if (type == ZL_CLOUD || type == ZL_BAND) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
+          if (type == ZL_CLOUD || type == ZL_BAND || masked(type)) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
           R = R2 * rinv;
           lg2R = lg2_ftz(R);
-          const float T = P.T0 * ex2_ftz(P.neg_delta * lg2R);  // blackbody.py:16-30
+          const float T = (L::generic ? C.T0 : P.T0) * ex2_ftz((L::generic ? C.neg_delta : P.neg_delta) * lg2R);  // blackbody.py:16-30
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) B[s] = bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
           if (P.has_scat) {  // scattering.py:11-59
@@ -200,7 +202,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           const float wc = lin_ff(hs_c[c], xk, wm_c[c]);
           Rc2 = fmaf(wc, wc, b2_c[c]);
           rcinv = rsqrt_ftz(Rc2);
-          if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
+          if (type == ZL_BAND || masked(type)) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
           Rc = Rc2 * rcinv;
           lg2Rc = 0.5f * lg2_ftz(Rc2);
         }
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           }
           t4s[c] = t4;
           dens = C.c[0] * rcinv * t2 * t3 * t4;
-        } else {  // ring (number_density.py:136-139) and feature (:167-181)
+        } else if (ringlike(type)) {  // ring (number_density.py:136-139) and feature (:167-181), RRM: x A
           float dR = Rc - C.c[1];
           if (precise) {
             // R^2 - R0^2 = w^2 + c' to ~1 ulp; one Newton step on R
@@ -243,11 +245,15 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
             dR = dR + (D2 - dR * (Rc + C.c[1])) * (0.5f * rcinv);
           }
           float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
-          if (type == ZL_FEATURE) {
+          if (featurelike(type)) {
             const float dth = atan2f(fmaf(fy1[c], xk.hi, fy0[c]), fmaf(fx1[c], xk.hi, fx0[c]));
             arg = fmaf(dth * dth, C.c[7], arg);
           }
           dens = C.c[0] * ex2_ftz(-arg);
+        } else if (type == ZL_INTERSTELLAR) {  // number_density.py:259-264
+          dens = C.c[0];
+        } else {
+          dens = rrm_masked_density(C, type, hs_c[c], xk, wm_c[c], cw_c[c], z1_c[c], z0_c[c], Z, rcinv, lg2Rc);
         }
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {

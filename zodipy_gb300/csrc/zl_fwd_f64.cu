@@ -10,7 +10,8 @@
 //   quadrature (sequential sum) .. zodipy/line_of_sight.py:55-61
 //   integrand .................... zodipy/brightness.py:21-56
 //   T(R), blackbody lookup ....... zodipy/blackbody.py:16-30, numpy.interp
-//   densities .................... zodipy/number_density.py:47-181
+//   densities .................... zodipy/number_density.py:47-181 (Kelsall), :184-404 (RRM)
+//   RRM integrand ................ zodipy/brightness.py:59-83
 //   scattering ................... zodipy/scattering.py:11-59
 //   total = sum over components .. zodipy/model.py:203
 #include "zl_common.cuh"
@@ -65,8 +66,10 @@ __device__ __forceinline__ double sphere_distance(double b, double r_obs, double
   return np_maximum(q, c / q);
 }
 
-// Number density of one Kelsall-98 component at heliocentric X (zodipy/number_density.py:47-181),
-// every expression in the reference's order; (ex, ey) is Earth's heliocentric x, y (feature only).
+// Number density of one component at heliocentric X (zodipy/number_density.py:47-404), every
+// expression in the reference's order; (ex, ey) is Earth's heliocentric x, y (features only).
+// The RRM densities are zero outside their radial mask, as the reference's filtered assignment
+// leaves them (a nan distance fails the mask too).
 __device__ __forceinline__ double density_f64(const ZlComponent& C, double X0, double X1, double X2, double ex,
                                               double ey) {
   // number_density.py: X - X_0, its norm, and the height above the symmetry plane
@@ -88,21 +91,53 @@ __device__ __forceinline__ double density_f64(const ZlComponent& C, double X0, d
     const double t4 = 1.0 - exp(-pow(Rc / C.p[3], 20.0));
     return t1 * t2 * t3 * t4;
   }
-  if (C.type == ZL_RING) {  // number_density.py:136-139
+  if (C.type == ZL_RING || C.type == ZL_RING_RRM) {  // number_density.py:136-139; RRM :345-370
     const double d = Rc - C.p[0];
     const double t1 = -(d * d) / (C.p[1] * C.p[1]);
     const double t2 = fabs(Zc) / C.p[2];
-    return C.n_0 * exp(t1 - t2);
+    const double n = C.n_0 * exp(t1 - t2);
+    return C.type == ZL_RING ? n : C.p[3] * n;
   }
-  // feature, number_density.py:167-181
-  const double te = atan2(ey - C.offset[1], ex - C.offset[0]);
-  double dth = (atan2(Xc1, Xc0) - te) - C.p[3];
-  dth = np_remainder(dth + kPi, 2.0 * kPi) - kPi;
-  const double d = Rc - C.p[0];
-  double e = d * d / (C.p[1] * C.p[1]);
-  e += fabs(Zc) / C.p[2];
-  e += dth * dth / (C.p[4] * C.p[4]);
-  return C.n_0 * exp(-e);
+  if (C.type == ZL_FEATURE || C.type == ZL_FEATURE_RRM) {  // number_density.py:167-181; RRM :373-403
+    const double te = atan2(ey - C.offset[1], ex - C.offset[0]);
+    double dth = (atan2(Xc1, Xc0) - te) - C.p[3];
+    dth = np_remainder(dth + kPi, 2.0 * kPi) - kPi;
+    const double d = Rc - C.p[0];
+    double e = d * d / (C.p[1] * C.p[1]);
+    e += fabs(Zc) / C.p[2];
+    e += dth * dth / (C.p[4] * C.p[4]);
+    const double n = C.n_0 * exp(-e);
+    return C.type == ZL_FEATURE ? n : C.p[5] * n;
+  }
+  if (C.type == ZL_INTERSTELLAR) return C.p[0];  // number_density.py:259-264
+  if (C.type == ZL_FAN) {  // number_density.py:184-218; p = gamma, Z_0, Q, P, R_outer
+    if (!(Rc <= C.p[4])) return 0.0;
+    const double beta = asin(Zc / Rc);
+    const double Zabs = fabs(Zc);
+    const double eps = Zabs < C.p[1] ? 2.0 - (Zabs / C.p[1]) : 1.0;
+    const double f = pow(cos(beta), C.p[2]) * exp(-C.p[3] * sin(pow(fabs(beta), eps)));
+    return pow(Rc, -C.p[0]) * f;
+  }
+  if (C.type == ZL_COMET) {  // number_density.py:221-256; p = gamma, Z_0, P, amp, R_inner, R_outer
+    if (!(Rc >= C.p[4] && Rc <= C.p[5])) return 0.0;
+    const double beta = asin(Zc / Rc);
+    const double Zabs = fabs(Zc);
+    const double eps = Zabs < C.p[1] ? 2.0 - (Zabs / C.p[1]) : 1.0;
+    const double f = exp(-C.p[2] * sin(pow(fabs(beta), eps)));
+    return C.p[3] * pow(Rc, -C.p[0]) * f;
+  }
+  if (C.type == ZL_NARROW_BAND) {  // number_density.py:267-304; p = gamma, A, G, R_inner, R_outer, beta_nb
+    if (!(Rc >= C.p[3] && Rc <= C.p[4])) return 0.0;
+    const double beta_abs = fabs(asin(Zc / Rc) * (180.0 / kPi));  // numpy.rad2deg
+    const double f = beta_abs < C.p[5] ? exp(C.p[2] * (beta_abs - C.p[5])) : 0.0;
+    return C.p[1] * pow(Rc / C.p[4], -C.p[0]) * f;
+  }
+  // broad band, number_density.py:307-342; p = gamma, A, R_inner, R_outer, beta_bb, sigma_bb
+  if (!(Rc >= C.p[2] && Rc <= C.p[3])) return 0.0;
+  const double beta = asin(Zc / Rc) * (180.0 / kPi);
+  const double a = (beta - C.p[4]) / C.p[5], b = (beta + C.p[4]) / C.p[5];
+  const double f = exp(-0.5 * (a * a)) + exp(-0.5 * (b * b));
+  return C.p[1] * pow(Rc / C.p[3], -C.p[0]) * f;
 }
 
 template <int NSPEC>
@@ -186,7 +221,7 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
           X1 = Xl1 + oy;
           X2 = Xl2 + oz;
           R = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
-          const double T = P.m.T_0 * pow(R, -P.m.delta);
+          const double T = P.range_T0[r] * pow(R, -P.range_delta[r]);
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) bb[s] = np_interp(T, xp, fp + s * nT, sl + s * nT, nT, x0, inv_dx);
           if (P.range_scat[r]) {  // scattering.py:26-31
@@ -197,6 +232,11 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
           hs_len = sp - st;
         }
         const double dens = density_f64(C, X0, X1, X2, O.earth[0], O.earth[1]);
+        if (P.m.family == ZL_RRM) {  // brightness.py:80-83
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) acc[c][s] += bb[s] * dens * P.m.spec[s].calibration * 0.5 * hs_len * wk;
+          continue;
+        }
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
           const double A = P.m.spec[s].albedo[c];

@@ -24,7 +24,10 @@ from .coords import SkyCoord as _LiteSkyCoord
 from .ephemeris import body_position
 from .spectral import blackbody_table, interp_spectral_param
 from .units import AU, MJy, Quantity, UnitConversionError, as_quantity, sr
-from .zodiacal_light_model import Kelsall, model_registry
+from .zodiacal_light_model import RRM, Kelsall, model_registry
+
+# (1 MJy / AU) in Jy / cm: the unit change of the RRM calibration (unpack_model.py:131-132)
+MJY_PER_AU_TO_JY_PER_CM = 1e6 / 1.495978707e13
 
 
 def _astropy():
@@ -102,13 +105,18 @@ class Model:
 
     # -- set-up -------------------------------------------------------------
     def _init_ipd_model_partials(self) -> None:
-        """Spectral unpacking (``unpack_model.py:23-107``) and kernel parameter block."""
+        """Spectral unpacking (``unpack_model.py:23-132``) and kernel parameter block."""
         self._interped_comp_params, self._interped_shared_params = self._unpack()
-        spec = {
-            "emissivity": [self._interped_comp_params[k]["emissivity"] for k in self._ipd_model.comps],
-            "albedo": [self._interped_comp_params[k]["albedo"] for k in self._ipd_model.comps],
-            **{k: self._interped_shared_params[k] for k in ("C1", "C2", "C3", "solar_irradiance")},
-        }
+        if isinstance(self._ipd_model, RRM):
+            n = self._ipd_model.ncomps
+            spec = {"emissivity": [0.0] * n, "albedo": [0.0] * n, "C1": 0.0, "C2": 0.0, "C3": 0.0}
+            spec.update(solar_irradiance=0.0, calibration=self._interped_shared_params["calibration"])
+        else:
+            spec = {
+                "emissivity": [self._interped_comp_params[k]["emissivity"] for k in self._ipd_model.comps],
+                "albedo": [self._interped_comp_params[k]["albedo"] for k in self._ipd_model.comps],
+                **{k: self._interped_shared_params[k] for k in ("C1", "C2", "C3", "solar_irradiance")},
+            }
         self._spectrum = spec
         self._zl_model = packing.pack_model(
             self._ipd_model, [spec], [self._b_nu_table], self._quad_points, self._quad_weights
@@ -123,6 +131,9 @@ class Model:
         def isp(table, nearest=False):
             return float(interp_spectral_param(xm, w, spectrum, table, use_nearest=nearest, bounds_error=self._bounds_error))
 
+        if isinstance(model, RRM):  # unpack_model.py:110-132
+            comp_params = {label: {"T_0": model.T_0[label], "delta": model.delta[label]} for label in model.comps}
+            return comp_params, {"calibration": isp(model.calibration) * MJY_PER_AU_TO_JY_PER_CM}
         comp_params = {}
         for label in model.comps:
             comp_params[label] = {

@@ -1,16 +1,30 @@
 """Published parameter sets of the built-in zodiacal light models.
 
 These are physical model constants, not code: the Kelsall et al. (1998)
-DIRBE fit and the Planck 2013/2015/2018 and Odegard et al. (2019) emissivity
-refits.  They must equal the values the reference ships
-(``zodipy/component_params.py:19-96``, ``zodipy/source_params.py:5-271``) so
+DIRBE fit, the Planck 2013/2015/2018 and Odegard et al. (2019) emissivity
+refits, and the Rowan-Robinson & May (2013) model.  They must equal the values
+the reference ships (``zodipy/component_params.py:19-204``,
+``zodipy/source_params.py:5-271``) so
 that outputs agree; ``tests/test_model_data.py`` checks them against a dump of
 the reference's own registry.
 """
 
 from __future__ import annotations
 
-from .components import Band, Cloud, ComponentLabel, Feature, Ring
+from .components import (
+    Band,
+    BroadBand,
+    Cloud,
+    Comet,
+    ComponentLabel,
+    Fan,
+    Feature,
+    FeatureRRM,
+    Interstellar,
+    NarrowBand,
+    Ring,
+    RingRRM,
+)
 
 L = ComponentLabel
 
@@ -115,6 +129,46 @@ T_0_DIRBE = 286.0
 DELTA_DIRBE = 0.46686259861486573
 
 DIRBE_BANDS_MICRON = [1.25, 2.2, 3.5, 4.9, 12.0, 25.0, 60.0, 100.0, 140.0, 240.0]
+IRAS_BANDS_MICRON = [12.0, 25.0, 60.0, 100.0]
+
+# Rowan-Robinson & May (2013): geometry (component_params.py:98-204), grain temperatures
+# (source_params.py:7-31) and the per-band calibration (source_params.py:37-39).
+R_MARS = 1.5237
+R_ASTEROID_BELT = 3.137
+R_KUIPER_BELT = 30.0
+_RRM_PLANE = dict(x_0=0.0, y_0=0.0, z_0=0.0, i=1.5, Omega=78.0)
+RRM_COMPONENTS = {
+    L.FAN: (Fan, dict(_RRM_PLANE, P=2.13, Q=10.7, gamma=1.3, Z_0=0.06, R_outer=R_MARS)),
+    L.COMET: (Comet, dict(_RRM_PLANE, P=2.5, gamma=1.0, Z_0=0.06, amp=0.37, R_inner=R_MARS, R_outer=R_KUIPER_BELT)),
+    L.INNER_NARROW_BAND: (
+        NarrowBand,
+        dict(_RRM_PLANE, A=0.04, gamma=1.0, beta_nb=9.35, G=0.12, R_inner=R_MARS, R_outer=R_ASTEROID_BELT),
+    ),
+    L.OUTER_NARROW_BAND: (
+        NarrowBand,
+        dict(_RRM_PLANE, A=0.032, gamma=1.0, beta_nb=1.42, G=0.6, R_inner=R_MARS, R_outer=R_ASTEROID_BELT),
+    ),
+    L.BROAD_BAND: (
+        BroadBand,
+        dict(x_0=0.0, y_0=0.0, z_0=0.0, i=2.6, Omega=110.0, A=0.051, gamma=1.0, beta_bb=9.3, sigma_bb=5.0,
+             R_inner=R_MARS, R_outer=R_ASTEROID_BELT),
+    ),
+    L.INTERSTELLAR: (Interstellar, dict(x_0=0.0, y_0=0.0, z_0=0.0, i=0.0, Omega=0.0, amp=0.010)),
+    L.RING_RRM: (
+        RingRRM,
+        dict(A=0.16, x_0=0.0, y_0=0.0, z_0=0.0, i=0.49, Omega=22.3, n_0=1.0, R=1.03, sigma_r=0.025, sigma_z=0.054),
+    ),
+    L.FEATURE_RRM: (
+        FeatureRRM,
+        dict(A=0.065, x_0=0.0, y_0=0.0, z_0=0.0, i=0.49, Omega=22.3, n_0=1.0, R=1.06, sigma_r=0.10, sigma_z=0.091,
+             theta=-10.0, sigma_theta=12.1),
+    ),
+}
+T_LARGE_GRAINS, T_SMALL_GRAINS = 255.0, 305.0
+DELTA_LARGE_GRAINS, DELTA_SMALL_GRAINS = 0.5, 0.4
+T_0_RRM = {lbl: (T_SMALL_GRAINS if lbl == L.INTERSTELLAR else T_LARGE_GRAINS) for lbl in RRM_COMPONENTS}
+DELTA_RRM = {lbl: (DELTA_SMALL_GRAINS if lbl == L.INTERSTELLAR else DELTA_LARGE_GRAINS) for lbl in RRM_COMPONENTS}
+CALIBRATION_RRM = [1.0, 1.0, 1.0, 1.0]
 PLANCK_BANDS_GHZ = [100.0, 143.0, 217.0, 353.0, 545.0, 857.0]
 
 _E_BAND_DIRBE = [

@@ -1,9 +1,10 @@
-"""Pack a Kelsall model and its spectral set-up into the C ABI's ``ZlModel``.
+"""Pack a model (Kelsall or RRM) and its spectral set-up into the C ABI's ``ZlModel``.
 
 Components keep their order (the reference's output order,
 ``zodipy/model.py:267-277``).  Components with identical (inner, outer)
-cutoffs share one line-of-sight range, so their node positions, temperature
-and blackbody value are computed once per node in the kernels.
+cutoffs -- and, for RRM, identical grain temperature law -- share one
+line-of-sight range, so their node positions, temperature and blackbody value
+are computed once per node in the kernels.
 """
 
 from __future__ import annotations
@@ -13,11 +14,39 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .components import COMPONENT_TYPE_CODE, Band, Cloud, Feature, Ring
-from .zodiacal_light_model import COMPONENT_CUTOFFS
+from .components import (
+    COMPONENT_TYPE_CODE,
+    Band,
+    BroadBand,
+    Cloud,
+    Comet,
+    Fan,
+    Feature,
+    FeatureRRM,
+    Interstellar,
+    NarrowBand,
+    Ring,
+    RingRRM,
+)
+from .zodiacal_light_model import COMPONENT_CUTOFFS, RRM
 
 
 def component_params(comp) -> list[float]:
+    """``ZlComponent.p`` of one component (order as in ``include/zodigb.h``)."""
+    if isinstance(comp, RingRRM):
+        return [comp.R, comp.sigma_r, comp.sigma_z, comp.A]
+    if isinstance(comp, FeatureRRM):
+        return [comp.R, comp.sigma_r, comp.sigma_z, comp.theta_rad, comp.sigma_theta_rad, comp.A]
+    if isinstance(comp, Fan):
+        return [comp.gamma, comp.Z_0, comp.Q, comp.P, comp.R_outer]
+    if isinstance(comp, Comet):
+        return [comp.gamma, comp.Z_0, comp.P, comp.amp, comp.R_inner, comp.R_outer]
+    if isinstance(comp, Interstellar):
+        return [comp.amp]
+    if isinstance(comp, NarrowBand):
+        return [comp.gamma, comp.A, comp.G, comp.R_inner, comp.R_outer, comp.beta_nb]
+    if isinstance(comp, BroadBand):
+        return [comp.gamma, comp.A, comp.R_inner, comp.R_outer, comp.beta_bb, comp.sigma_bb]
     if isinstance(comp, Cloud):
         return [comp.alpha, comp.beta, comp.gamma, comp.mu]
     if isinstance(comp, Band):
@@ -33,8 +62,9 @@ def pack_model(ipd_model, spectra: list[dict], bb_tables: list[np.ndarray], gl_x
     """Build the ``ZlModel`` for ``len(spectra)`` fused spectral sets.
 
     ``spectra[s]`` holds ``emissivity``/``albedo`` (one per component, model
-    order) and the scalars ``C1``, ``C2``, ``C3``, ``solar_irradiance``;
-    ``bb_tables[s]`` is the (2, n_T) blackbody table.
+    order) and the scalars ``C1``, ``C2``, ``C3``, ``solar_irradiance`` (and
+    ``calibration`` for an RRM model); ``bb_tables[s]`` is the (2, n_T)
+    blackbody table.
     """
     comps = list(ipd_model.comps.items())
     if not 1 <= len(comps) <= _lib.ZL_MAX_COMPS:
@@ -55,25 +85,37 @@ def pack_model(ipd_model, spectra: list[dict], bb_tables: list[np.ndarray], gl_x
     m.n_spec = len(spectra)
     m.n_nodes = gl_x.size
     m.n_temps = temps.size
-    m.T_0 = float(ipd_model.T_0)
-    m.delta = float(ipd_model.delta)
-    ranges: list[tuple[float, float]] = []
+    rrm = isinstance(ipd_model, RRM)
+    m.family = _lib.ZL_RRM if rrm else _lib.ZL_KELSALL
+    if rrm:
+        for c, (label, _) in enumerate(comps):
+            m.comp_T_0[c] = float(ipd_model.T_0[label])
+            m.comp_delta[c] = float(ipd_model.delta[label])
+    else:
+        m.T_0 = float(ipd_model.T_0)
+        m.delta = float(ipd_model.delta)
+    ranges: list[tuple] = []
+    cutoffs: list[tuple[float, float]] = []
     for c, (label, comp) in enumerate(comps):
         cut = tuple(float(v) for v in COMPONENT_CUTOFFS[label])
-        if cut not in ranges:
-            ranges.append(cut)
+        key = (cut, m.comp_T_0[c], m.comp_delta[c]) if rrm else cut
+        if key not in ranges:
+            ranges.append(key)
+            cutoffs.append(cut)
         k = m.comp[c]
         k.type = COMPONENT_TYPE_CODE[type(comp)]
-        k.range = ranges.index(cut)
+        k.range = ranges.index(key)
         k.offset[:] = [float(v) for v in comp.X_0]
         k.sin_i, k.cos_i = comp.sin_i_rad, comp.cos_i_rad
         k.sin_Omega, k.cos_Omega = comp.sin_Omega_rad, comp.cos_Omega_rad
-        k.n_0 = float(comp.n_0)
+        k.n_0 = float(getattr(comp, "n_0", 1.0))
         p = component_params(comp)
         for j, v in enumerate(p):
             k.p[j] = float(v)
+    if len(ranges) > _lib.ZL_MAX_RANGES:
+        raise ValueError(f"models with {len(ranges)} distinct line-of-sight ranges are not supported")
     m.n_ranges = len(ranges)
-    for r, (lo, hi) in enumerate(ranges):
+    for r, (lo, hi) in enumerate(cutoffs):
         m.cutoff[r][0] = lo
         m.cutoff[r][1] = hi
     m.temps[: temps.size] = temps.tolist()
@@ -90,6 +132,7 @@ def pack_model(ipd_model, spectra: list[dict], bb_tables: list[np.ndarray], gl_x
         ks.C2 = float(sp["C2"])
         ks.C3 = float(sp["C3"])
         ks.solar_irradiance = float(sp["solar_irradiance"])
+        ks.calibration = float(sp.get("calibration", 0.0))
         ks.bb[: temps.size] = np.asarray(tab[1], dtype=np.float64).tolist()
     lib = _lib.load()
     _lib.check(lib.zl_model_check(ctypes.byref(m)), "zl_model_check")

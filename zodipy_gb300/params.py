@@ -29,12 +29,19 @@ _OWN = {
 _DEG = {(_lib.ZL_BAND, 0), (_lib.ZL_FEATURE, 3), (_lib.ZL_FEATURE, 4)}
 
 
+def _own(t) -> tuple:
+    try:
+        return _OWN[t]
+    except KeyError:
+        raise ValueError("the adjoint covers the Kelsall component types (cloud, band, ring, feature) only") from None
+
+
 def names(zl_model, labels) -> list[str]:
     out = []
     for c in range(zl_model.n_comps):
         t = zl_model.comp[c].type
         lab = labels[c]
-        out += [f"comps.{lab}.{k}" for k in ("x_0", "y_0", "z_0", "i", "Omega", "n_0", *_OWN[t])]
+        out += [f"comps.{lab}.{k}" for k in ("x_0", "y_0", "z_0", "i", "Omega", "n_0", *_own(t))]
     out += ["T_0", "delta"]
     for s in range(zl_model.n_spec):
         sfx = f"[{s}]" if zl_model.n_spec > 1 else ""
@@ -51,7 +58,7 @@ def vector_from_model(m) -> np.ndarray:
         inc = math.degrees(math.atan2(k.sin_i, k.cos_i))
         node = math.degrees(math.atan2(k.sin_Omega, k.cos_Omega))
         v += [k.offset[0], k.offset[1], k.offset[2], inc, node, k.n_0]
-        for j in range(len(_OWN[k.type])):
+        for j in range(len(_own(k.type))):
             v.append(math.degrees(k.p[j]) if (k.type, j) in _DEG else k.p[j])
     v += [m.T_0, m.delta]
     for s in range(m.n_spec):
@@ -75,7 +82,7 @@ def model_from_vector(base, vec) -> "_lib.ZlModel":
         k.sin_Omega, k.cos_Omega = math.sin(node), math.cos(node)
         k.n_0 = vec[j + 5]
         j += 6
-        for q in range(len(_OWN[k.type])):
+        for q in range(len(_own(k.type))):
             k.p[q] = math.radians(vec[j]) if (k.type, q) in _DEG else vec[j]
             j += 1
     m.T_0, m.delta = vec[j], vec[j + 1]
@@ -95,4 +102,4 @@ def model_from_vector(base, vec) -> "_lib.ZlModel":
 
 
 def size(m) -> int:
-    return sum(6 + len(_OWN[m.comp[c].type]) for c in range(m.n_comps)) + 2 + m.n_spec * (2 * m.n_comps + 4)
+    return sum(6 + len(_own(m.comp[c].type)) for c in range(m.n_comps)) + 2 + m.n_spec * (2 * m.n_comps + 4)

@@ -1,6 +1,6 @@
-"""Kelsall-type model definitions and the model registry.
+"""Model definitions (Kelsall, RRM) and the model registry.
 
-Mirrors the reference's ``Kelsall`` dataclass and ``ModelRegistry``
+Mirrors the reference's ``Kelsall`` / ``RRM`` dataclasses and ``ModelRegistry``
 (``zodipy/zodiacal_light_model.py:20-142``, ``zodipy/model_registry.py:4-62``)
 so that ``get_parameters()`` / ``update_parameters()`` dictionaries have the
 same structure and keys.
@@ -19,10 +19,11 @@ from .components import ComponentLabel, ZodiacalComponent
 from .units import GHz, Quantity, UnitConversionError, as_quantity, micron, spectral
 
 # Per-component (inner, outer) cutoff radii of the line of sight
-# (zodipy/line_of_sight.py:14-26).
+# (zodipy/line_of_sight.py:14-52).
 R_0 = float(np.finfo(np.float64).eps)
 R_JUPITER = 5.2
 R_EARTH = 1.0
+_RRM = {lbl: cls(**kw) for lbl, (cls, kw) in md.RRM_COMPONENTS.items()}
 COMPONENT_CUTOFFS = {
     ComponentLabel.CLOUD: (R_0, R_JUPITER),
     ComponentLabel.BAND1: (R_0, R_JUPITER),
@@ -30,6 +31,21 @@ COMPONENT_CUTOFFS = {
     ComponentLabel.BAND3: (R_0, R_JUPITER),
     ComponentLabel.RING: (R_EARTH - 0.2, R_EARTH + 0.2),
     ComponentLabel.FEATURE: (R_EARTH - 0.3, R_EARTH + 0.3),
+    # RRM: the cutoffs of the built-in parameters, fixed at import like the reference's
+    ComponentLabel.FAN: (R_0, _RRM[ComponentLabel.FAN].R_outer),
+    ComponentLabel.INNER_NARROW_BAND: (
+        _RRM[ComponentLabel.INNER_NARROW_BAND].R_inner,
+        _RRM[ComponentLabel.INNER_NARROW_BAND].R_outer,
+    ),
+    ComponentLabel.OUTER_NARROW_BAND: (
+        _RRM[ComponentLabel.OUTER_NARROW_BAND].R_inner,
+        _RRM[ComponentLabel.OUTER_NARROW_BAND].R_outer,
+    ),
+    ComponentLabel.BROAD_BAND: (_RRM[ComponentLabel.BROAD_BAND].R_inner, _RRM[ComponentLabel.BROAD_BAND].R_outer),
+    ComponentLabel.COMET: (_RRM[ComponentLabel.COMET].R_inner, _RRM[ComponentLabel.COMET].R_outer),
+    ComponentLabel.INTERSTELLAR: (R_0, md.R_KUIPER_BELT),
+    ComponentLabel.RING_RRM: (R_EARTH - 0.2, R_EARTH + 0.2),
+    ComponentLabel.FEATURE_RRM: (R_EARTH - 0.3, R_EARTH + 0.3),
 }
 
 
@@ -78,6 +94,15 @@ class Kelsall(ZodiacalLightModel):
     C1: Sequence[float] | None = None
     C2: Sequence[float] | None = None
     C3: Sequence[float] | None = None
+
+
+@dataclass(repr=False)
+class RRM(ZodiacalLightModel):
+    """Rowan-Robinson & May (2013) model family: grain temperature per component, one calibration."""
+
+    T_0: Mapping[ComponentLabel, float]
+    delta: Mapping[ComponentLabel, float]
+    calibration: Sequence[float]
 
 
 @dataclass
@@ -143,6 +168,16 @@ def _registry() -> ModelRegistry:
                 emissivities=copy.deepcopy(emis),
             ),
         )
+    reg.register_model(
+        "rrm-experimental",
+        RRM(
+            comps=_components(md.RRM_COMPONENTS),
+            spectrum=Quantity(md.IRAS_BANDS_MICRON, micron),
+            calibration=list(md.CALIBRATION_RRM),
+            T_0=dict(md.T_0_RRM),
+            delta=dict(md.DELTA_RRM),
+        ),
+    )
     return reg
 
 
