@@ -165,6 +165,20 @@ ZL_API int zl_forward(const ZlModel* model, const double* unit_vectors_dev, int6
                const ZlObserver* observers_dev, int32_t n_obs, int32_t precision,
                double* out_comps_dev, double* out_total_dev, void* stream);
 
+/* Forward pass for time-ordered data: one observer and one Earth position per
+ * pixel (zodipy/model.py:119-203 with obstime.size == n_pix and obspos of shape
+ * (3, n_pix)).  Replaces the same loop as zl_forward; the cutoff rule of
+ * line_of_sight.py:72-73 is applied to the whole call (a range collapses to
+ * eps for every pixel when any sample's observer lies outside it), as the
+ * reference does.
+ *  obs_xyz_dev, earth_xyz_dev: float64 [3][n_pix] heliocentric ecliptic [AU];
+ *      earth_xyz_dev may be NULL when no component is a feature
+ *  flags_dev: one uint32_t of device scratch; it receives the OR of the
+ *      samples' cutoff flags (it is zeroed and filled on `stream` first) */
+ZL_API int zl_forward_tod(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+                          const double* obs_xyz_dev, const double* earth_xyz_dev, uint32_t* flags_dev,
+                          int32_t precision, double* out_comps_dev, double* out_total_dev, void* stream);
+
 /* ---- Adjoint -------------------------------------------------------------
  * Gradient of a loss L with respect to every model parameter, given the
  * upstream gradient dL/d(output) of the float32 forward pass (no counterpart
@@ -211,6 +225,44 @@ ZL_API int zl_backward(const ZlModel* model, const double* unit_vectors_dev, int
 ZL_API int zl_backward_static(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
                               const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
                               const double* g_total_dev, double* grad_out_dev, void* stream);
+
+/* zl_backward for time-ordered data (positions and flags as zl_forward_tod). */
+ZL_API int zl_backward_tod(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+                           const double* obs_xyz_dev, const double* earth_xyz_dev, uint32_t* flags_dev,
+                           const double* g_comps_dev, const double* g_total_dev, double* grad_out_dev,
+                           void* workspace_dev, size_t workspace_bytes, void* stream);
+
+/* ---- Time-ordered inputs on the device (zodipy/model.py:177-180, bodies.py:16-50) ---- */
+
+/* Positions at n sample times from a cubic spline through n_knots ascending
+ * knots: replaces the evaluation of scipy's CubicSpline in
+ * get_interp_bodypos (bodies.py:22-35).  coef_dev is the piecewise polynomial
+ * the host builds over the knots, float64 [4][n_knots-1][3] with the cubic
+ * coefficient first (scipy's PPoly.c layout for a (3, n_knots) array
+ * interpolated along its last axis).  The value at t is the power sum of
+ * interval j (knots[j] <= t < knots[j+1]; ends extrapolate), accumulated from
+ * the constant term up as scipy does.  out_dev: float64 [3][n]. */
+ZL_API int zl_spline_eval(const double* knots_dev, int32_t n_knots, const double* coef_dev, const double* t_dev,
+                          int64_t n, double* out_dev, void* stream);
+
+#define ZL_SEMB_L2_SCRATCH 1024 /* doubles of scratch zl_semb_l2 needs with whole_array_norm */
+
+/* SEMB-L2 observer (bodies.py:38-50): Earth's direction from the Sun scaled
+ * to |E| + l2_distance.  With whole_array_norm == 0, |E| is each sample's own
+ * distance (the reference's result for a single time); with whole_array_norm
+ * != 0, |E| is the norm of the whole [3][n] array, which is what the
+ * reference's numpy.linalg.norm(earthpos) computes for a sequence of times.
+ * The second form needs scratch_dev of ZL_SEMB_L2_SCRATCH doubles. */
+ZL_API int zl_semb_l2(const double* earth_xyz_dev, int64_t n, double l2_distance, int32_t whole_array_norm,
+                      double* scratch_dev, int64_t scratch_len, double* out_dev, void* stream);
+
+/* Unit vectors of (lon, lat) [rad] rotated into the ecliptic frame:
+ * u = R (cos lat cos lon, cos lat sin lon, sin lat), R a row-major 3x3 host
+ * matrix (NULL = identity).  Replaces the frame transform of model.py:244-251
+ * for frames that differ from the ecliptic by a fixed rotation (ICRS,
+ * Galactic).  unit_vectors_dev: float64 [3][n]. */
+ZL_API int zl_directions(const double* lon_dev, const double* lat_dev, int64_t n, const double* rotation_host,
+                         double* unit_vectors_dev, void* stream);
 
 /* Number densities of every component on a Cartesian mesh, float64
  * (replaces the evaluation loop of zodipy/number_density.py:482-536).

@@ -22,6 +22,7 @@ ZL_MAX_TEMPS = 128
 ZL_CLOUD, ZL_BAND, ZL_RING, ZL_FEATURE = 0, 1, 2, 3
 ZL_FAN, ZL_COMET, ZL_INTERSTELLAR, ZL_NARROW_BAND, ZL_BROAD_BAND, ZL_RING_RRM, ZL_FEATURE_RRM = 4, 5, 6, 7, 8, 9, 10
 ZL_KELSALL, ZL_RRM = 0, 1
+ZL_SEMB_L2_SCRATCH = 1024
 ZL_PREC_F64, ZL_PREC_F32 = 0, 1
 ZL_OK, ZL_ERR_ARG, ZL_ERR_CUDA, ZL_ERR_MODEL, ZL_ERR_SPACE = 0, -1, -2, -3, -4
 
@@ -109,6 +110,31 @@ _SIGNATURES = {
         ],
     ),
     "zl_set_launch": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "zl_forward_tod": (
+        ctypes.c_int,
+        [ctypes.POINTER(ZlModel), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    ),
+    "zl_backward_tod": (
+        ctypes.c_int,
+        [ctypes.POINTER(ZlModel), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "zl_spline_eval": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_void_p],
+    ),
+    "zl_semb_l2": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+         ctypes.c_void_p, ctypes.c_void_p],
+    ),
+    "zl_directions": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+         ctypes.c_void_p],
+    ),
     "zl_density_grid": (
         ctypes.c_int,
         [

@@ -84,6 +84,14 @@ class SkyCoord:
     def size(self) -> int:
         return int(np.size(self.lon))
 
+    def ecliptic_rotation(self) -> np.ndarray:
+        """3x3 matrix from this frame's Cartesian axes to the ecliptic ones."""
+        if self.frame == "icrs":
+            return _EQ_TO_ECL
+        if self.frame == "galactic":
+            return _EQ_TO_ECL @ _GAL_TO_EQ
+        return np.eye(3)
+
     def ecliptic_unit_vectors(self) -> np.ndarray:
         """(3, n) heliocentric-ecliptic unit vectors of the directions."""
         cl = np.cos(self.lat)

@@ -12,17 +12,19 @@
 #include "zl_common.cuh"
 
 namespace zl {
-cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ZlObserver* obs, int n_obs,
+cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
                            double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
 cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
-                           const ZlObserver* obs, int n_obs, double* oc, double* ot, cudaStream_t st, int tpb,
+                           const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb,
                            int bps, int num_sms);
 int grad_count_layout(int layout, int n_spec);
 int bwd_groups(int layout);
 cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
-                           const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                           const ObsArgs& obs, const double* g_comps, const double* g_total,
                            double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms);
 cudaError_t launch_reduce_tiles(const double* partials, int64_t n_rows, int ng, double* out, cudaStream_t st);
+cudaError_t launch_tod_flags(const ZlModel& m, const double* obs, int64_t n, uint32_t* flags, cudaStream_t st,
+                             int num_sms);
 cudaError_t launch_density_grid(const ZlModel& M, const double* x, int nx, const double* y, int ny, const double* z,
                                 int nz, double ex, double ey, double* out, cudaStream_t st, int num_sms);
 }  // namespace zl
@@ -377,14 +379,13 @@ extern "C" ZL_API int zl_debug_plain_geometry(int32_t on) {
   return ZL_OK;
 }
 
-extern "C" ZL_API int zl_forward(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs, int32_t n_obs,
-                          int32_t precision, double* out_comps, double* out_total, void* stream) {
-  int rc = zl_model_check(model);
-  if (rc) return rc;
-  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
-  if (n_pix == 0) return ZL_OK;
+namespace {
+
+// zl_forward / zl_forward_tod after the observer source is set up.
+int forward_impl(const ZlModel* model, const double* u, int64_t n_pix, const ObsArgs& OA, int32_t precision,
+                 double* out_comps, double* out_total, void* stream) {
+  int rc = 0;
   if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
-  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
   if (!out_comps && !out_total) return fail(ZL_ERR_ARG, "both outputs are NULL");
   if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
   int nsm = 0;
@@ -400,16 +401,64 @@ extern "C" ZL_API int zl_forward(const ZlModel* model, const double* u, int64_t 
     static thread_local KParamsF64 P;
     build_f64(*model, &P);
     const int bps = cfg.bps ? cfg.bps : 8;
-    e = launch_fwd_f64(P, u, n_pix, obs, n_obs, out_comps, out_total, st, cfg.tpb, bps, nsm);
+    e = launch_fwd_f64(P, u, n_pix, OA, out_comps, out_total, st, cfg.tpb, bps, nsm);
   } else {
     static thread_local KParamsF32 P;
     build_f32(*model, &P);
     const int bps = cfg.bps ? cfg.bps : 8;
-    e = launch_fwd_f32(P, detect_layout(*model), g_plain_geometry != 0, u, n_pix, obs, n_obs, out_comps, out_total,
-                       st, cfg.tpb, bps, nsm);
+    e = launch_fwd_f32(P, detect_layout(*model), g_plain_geometry != 0, u, n_pix, OA, out_comps, out_total, st,
+                       cfg.tpb, bps, nsm);
   }
   if (e != cudaSuccess) return cuda_fail(e, "zl_forward launch");
   return ZL_OK;
+}
+
+bool needs_earth(const ZlModel& m) {
+  for (int c = 0; c < m.n_comps; ++c)
+    if (featurelike(m.comp[c].type)) return true;
+  return false;
+}
+
+// Checks and flag reduction shared by the time-ordered entry points.
+int tod_setup(const ZlModel* model, int64_t n_pix, const double* obs_xyz, const double* earth_xyz, uint32_t* flags,
+              void* stream, ObsArgs* OA) {
+  if (!obs_xyz || !flags) return fail(ZL_ERR_ARG, "obs_xyz or flags is NULL");
+  if (!earth_xyz && needs_earth(*model)) return fail(ZL_ERR_ARG, "earth_xyz is NULL but the model has a feature");
+  int nsm = 0, rc = 0;
+  if ((rc = sm_count(&nsm))) return rc;
+  cudaError_t e = launch_tod_flags(*model, obs_xyz, n_pix, flags, (cudaStream_t)stream, nsm);
+  if (e != cudaSuccess) return cuda_fail(e, "cutoff flags launch");
+  *OA = ObsArgs{nullptr, 0, obs_xyz, earth_xyz, flags};
+  return ZL_OK;
+}
+
+}  // namespace
+
+extern "C" ZL_API int zl_forward(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs, int32_t n_obs,
+                          int32_t precision, double* out_comps, double* out_total, void* stream) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
+  if (n_pix == 0) return ZL_OK;
+  if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  const ObsArgs OA{obs, n_obs, nullptr, nullptr, nullptr};
+  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, stream);
+}
+
+extern "C" ZL_API int zl_forward_tod(const ZlModel* model, const double* u, int64_t n_pix, const double* obs_xyz,
+                                     const double* earth_xyz, uint32_t* flags, int32_t precision, double* out_comps,
+                                     double* out_total, void* stream) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
+  if (n_pix == 0) return ZL_OK;
+  if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
+  if (!out_comps && !out_total) return fail(ZL_ERR_ARG, "both outputs are NULL");
+  if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
+  ObsArgs OA;
+  if ((rc = tod_setup(model, n_pix, obs_xyz, earth_xyz, flags, stream, &OA))) return rc;
+  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -510,18 +559,12 @@ extern "C" ZL_API int zl_backward_workspace_bytes(const ZlModel* model, int64_t 
   return ZL_OK;
 }
 
-extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs,
-                                  int32_t n_obs, const double* g_comps, const double* g_total, double* grad_out,
-                                  void* workspace, size_t workspace_bytes, void* stream) {
-  int rc = zl_model_check(model);
-  if (rc) return rc;
-  int layout = 0;
-  if ((rc = bwd_layout(*model, &layout))) return rc;
-  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
-  if (!grad_out) return fail(ZL_ERR_ARG, "grad_out is NULL");
-  if (n_pix > 0 && !u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
-  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
-  if ((g_comps == nullptr) == (g_total == nullptr)) return fail(ZL_ERR_ARG, "pass exactly one of g_comps, g_total");
+namespace {
+
+int backward_impl(const ZlModel* model, int layout, const double* u, int64_t n_pix, const ObsArgs& OA,
+                  const double* g_comps, const double* g_total, double* grad_out, void* workspace,
+                  size_t workspace_bytes, void* stream) {
+  int rc = 0;
   size_t need = 0;
   if ((rc = zl_backward_workspace_bytes(model, n_pix, &need))) return rc;
   if (workspace_bytes < need || (need > 0 && !workspace))
@@ -543,12 +586,48 @@ extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t
   build_f32(*model, &P);
   build_aux(*model, &A);
   cudaError_t e = cudaSuccess;
-  if (n_tiles > 0)
-    e = launch_bwd_f32(P, A, layout, u, n_pix, obs, n_obs, g_comps, g_total, partials, n_tiles, st, bps, nsm);
+  if (n_tiles > 0) e = launch_bwd_f32(P, A, layout, u, n_pix, OA, g_comps, g_total, partials, n_tiles, st, bps, nsm);
   if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
   e = launch_reduce_tiles(partials, n_tiles * bwd_groups(layout), ng, grad_out, st);
   if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
   return ZL_OK;
+}
+
+int backward_args(const ZlModel* model, const double* u, int64_t n_pix, const double* g_comps, const double* g_total,
+                  double* grad_out, int* layout) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if ((rc = bwd_layout(*model, layout))) return rc;
+  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
+  if (!grad_out) return fail(ZL_ERR_ARG, "grad_out is NULL");
+  if (n_pix > 0 && !u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
+  if ((g_comps == nullptr) == (g_total == nullptr)) return fail(ZL_ERR_ARG, "pass exactly one of g_comps, g_total");
+  return ZL_OK;
+}
+
+}  // namespace
+
+extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs,
+                                  int32_t n_obs, const double* g_comps, const double* g_total, double* grad_out,
+                                  void* workspace, size_t workspace_bytes, void* stream) {
+  int layout = 0;
+  int rc = backward_args(model, u, n_pix, g_comps, g_total, grad_out, &layout);
+  if (rc) return rc;
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  const ObsArgs OA{obs, n_obs, nullptr, nullptr, nullptr};
+  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, stream);
+}
+
+extern "C" ZL_API int zl_backward_tod(const ZlModel* model, const double* u, int64_t n_pix, const double* obs_xyz,
+                                      const double* earth_xyz, uint32_t* flags, const double* g_comps,
+                                      const double* g_total, double* grad_out, void* workspace,
+                                      size_t workspace_bytes, void* stream) {
+  int layout = 0;
+  int rc = backward_args(model, u, n_pix, g_comps, g_total, grad_out, &layout);
+  if (rc) return rc;
+  ObsArgs OA{nullptr, 0, nullptr, nullptr, nullptr};
+  if (n_pix > 0 && (rc = tod_setup(model, n_pix, obs_xyz, earth_xyz, flags, stream, &OA))) return rc;
+  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -65,7 +65,7 @@ template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT>
 __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                         const __grid_constant__ KGradAux A,
                                                         const double* __restrict__ u, int64_t n_pix,
-                                                        const ZlObserver* __restrict__ observers, int n_obs,
+                                                        const ObsArgs OA,
                                                         const double* __restrict__ g_comps,
                                                         const double* __restrict__ g_total,
                                                         double* __restrict__ partials, int64_t n_tiles) {
@@ -89,8 +89,8 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
     if (i < n_pix) {
       // ---- per-pixel set-up (as the forward kernel) ---------------------------
       const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
-      const ZlObserver& O = observers[find_observer(observers, n_obs, i)];
-      const ff ox = ff_from_double(O.obs[0]), oy = ff_from_double(O.obs[1]), oz = ff_from_double(O.obs[2]);
+      const PixObs O = pixel_observer(OA, i, n_pix);
+      const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
       const uint32_t outside = O.outside;
       const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
       const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           cw_c[c] = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
         }
         if (type == ZL_FEATURE) {
-          const float ex = (float)(O.earth[0] - (double)C.ox), ey = (float)(O.earth[1] - (double)C.oy);
+          const float ex = (float)(O.ex - (double)C.ox), ey = (float)(O.ey - (double)C.oy);
           const float phi = atan2f(ey, ex) + C.c[6];
           float sp, cp;
           sincosf(phi, &sp, &cp);
@@ -390,27 +390,27 @@ int bwd_groups(int layout) { return layout == 1 ? 2 : 1; }
 
 template <uint32_t LAYOUT, uint32_t MASK, int NSPEC>
 static void launch_one(bool scat, const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
-                       const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                       const ObsArgs& obs, const double* g_comps, const double* g_total,
                        double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
   if (scat)
     bwd_f32_kernel<LAYOUT, MASK, NSPEC, true>
-        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles);
+        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles);
   else
     bwd_f32_kernel<LAYOUT, MASK, NSPEC, false>
-        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles);
+        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles);
 }
 
 template <uint32_t LAYOUT, int NSPEC>
 static cudaError_t launch_groups(const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
-                                 const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                                 const ObsArgs& obs, const double* g_comps, const double* g_total,
                                  double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
   const bool scat = P.has_scat != 0;
-  launch_one<LAYOUT, 0x0Fu, NSPEC>(scat, P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles, st, grid);
+  launch_one<LAYOUT, 0x0Fu, NSPEC>(scat, P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
   if constexpr (LAYOUT == kLayoutDirbe) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     constexpr int NG = GradLay<LAYOUT, NSPEC>::NG;
-    launch_one<LAYOUT, 0x30u, NSPEC>(scat, P, A, u, n, obs, n_obs, g_comps, g_total,
+    launch_one<LAYOUT, 0x30u, NSPEC>(scat, P, A, u, n, obs, g_comps, g_total,
                                      partials + (size_t)n_tiles * NG, n_tiles, st, grid);
   }
   return cudaGetLastError();
@@ -418,13 +418,13 @@ static cudaError_t launch_groups(const KParamsF32& P, const KGradAux& A, const d
 
 // partials: [bwd_groups(layout)][n_tiles][grad_count_layout(layout, n_spec)]
 cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
-                           const ZlObserver* obs, int n_obs, const double* g_comps, const double* g_total,
+                           const ObsArgs& obs, const double* g_comps, const double* g_total,
                            double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms) {
   int64_t grid = (int64_t)num_sms * bps;
   if (grid > n_tiles) grid = n_tiles;
   if (grid < 1) grid = 1;
 #define ZL_BWD_CASE(LAY, NS) \
-  return launch_groups<LAY, NS>(P, A, u, n, obs, n_obs, g_comps, g_total, partials, n_tiles, st, grid)
+  return launch_groups<LAY, NS>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid)
   if (layout == 1) {
     switch (P.n_spec) {
       case 1: ZL_BWD_CASE(kLayoutDirbe, 1);

@@ -224,4 +224,41 @@ __device__ __forceinline__ int find_observer(const ZlObserver* __restrict__ obs,
   return lo;
 }
 
+// Where a kernel finds pixel i's observer: sorted ZlObserver records (one per
+// instant, rec != NULL), or time-ordered positions, one per pixel, as float64
+// [3][n_pix] arrays with a single cutoff-flag word for the whole call.
+struct ObsArgs {
+  const ZlObserver* rec;
+  int32_t n_rec;
+  const double* obs;     // [3][n_pix] (time-ordered) or NULL
+  const double* earth;   // [3][n_pix] or NULL (then Earth is only needed by no component)
+  const uint32_t* flags; // time-ordered: the OR of every sample's cutoff flags
+};
+
+struct PixObs {
+  double ox, oy, oz, ex, ey;
+  uint32_t outside;
+};
+
+__device__ __forceinline__ PixObs pixel_observer(const ObsArgs& A, int64_t i, int64_t n_pix) {
+  PixObs p;
+  if (A.rec) {
+    const ZlObserver& O = A.rec[find_observer(A.rec, A.n_rec, i)];
+    p.ox = O.obs[0];
+    p.oy = O.obs[1];
+    p.oz = O.obs[2];
+    p.ex = O.earth[0];
+    p.ey = O.earth[1];
+    p.outside = O.outside;
+  } else {
+    p.ox = A.obs[i];
+    p.oy = A.obs[n_pix + i];
+    p.oz = A.obs[2 * n_pix + i];
+    p.ex = A.earth ? A.earth[i] : 0.0;
+    p.ey = A.earth ? A.earth[n_pix + i] : 0.0;
+    p.outside = __ldg(A.flags);
+  }
+  return p;
+}
+
 }  // namespace zl

@@ -33,7 +33,7 @@ namespace zl {
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE>
 __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                       const double* __restrict__ u, int64_t n_pix,
-                                                      const ZlObserver* __restrict__ observers, int n_obs,
+                                                      const ObsArgs OA,
                                                       double* __restrict__ out_comps, double* __restrict__ out_total) {
   using L = Lay<LAYOUT>;
   constexpr int NC = L::ncomp();
@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
     // ---- per-pixel set-up -------------------------------------------------
     const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
-    const ZlObserver& O = observers[find_observer(observers, n_obs, i)];
-    const ff ox = ff_from_double(O.obs[0]), oy = ff_from_double(O.obs[1]), oz = ff_from_double(O.obs[2]);
+    const PixObs O = pixel_observer(OA, i, n_pix);
+    const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
     const uint32_t outside = O.outside;
     const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
     const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
         // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
         // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
         // two coordinates that are linear in the node abscissa
-        const float phi = atan2f((float)(O.earth[1] - (double)C.oy), (float)(O.earth[0] - (double)C.ox)) + C.c[6];
+        const float phi = atan2f((float)(O.ey - (double)C.oy), (float)(O.ex - (double)C.ox)) + C.c[6];
         float sp, cp;
         sincosf(phi, &sp, &cp);
         const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
@@ -284,39 +284,39 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 }
 
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE>
-static cudaError_t launch_f32_t(const KParamsF32& P, const double* u, int64_t n, const ZlObserver* obs, int n_obs,
+static cudaError_t launch_f32_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
                                 double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
   const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
   const int64_t blocks_needed = (n + tpb - 1) / tpb;
   int64_t grid = (int64_t)num_sms * bps;
   if (grid > blocks_needed) grid = blocks_needed;
   if (grid < 1) grid = 1;
-  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, n_obs, oc, ot);
+  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
   return cudaGetLastError();
 }
 
 template <uint32_t LAYOUT>
-static cudaError_t launch_f32_layout(const KParamsF32& P, const double* u, int64_t n, const ZlObserver* obs,
-                                     int n_obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+static cudaError_t launch_f32_layout(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
+                                     double* oc, double* ot, cudaStream_t st, int tpb, int bps,
                                      int num_sms) {
   switch (P.n_spec) {
-    case 1: return launch_f32_t<1, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-    case 2: return launch_f32_t<2, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-    case 3: return launch_f32_t<3, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-    default: return launch_f32_t<4, LAYOUT, true>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+    case 1: return launch_f32_t<1, LAYOUT, true>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 2: return launch_f32_t<2, LAYOUT, true>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 3: return launch_f32_t<3, LAYOUT, true>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    default: return launch_f32_t<4, LAYOUT, true>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
   }
 }
 
 // layout: 1 = DIRBE-like, 2 = Planck-like, 0 = generic; plain_geometry selects the
 // all-float32 variant of the DIRBE layout (kept for the precision/speed study).
 cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
-                           const ZlObserver* obs, int n_obs, double* oc, double* ot, cudaStream_t st, int tpb,
+                           const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb,
                            int bps, int num_sms) {
   if (layout == 1 && plain_geometry && P.n_spec == 1)
-    return launch_f32_t<1, kLayoutDirbe, false>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-  if (layout == 1) return launch_f32_layout<kLayoutDirbe>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-  if (layout == 2) return launch_f32_layout<kLayoutPlanck>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-  return launch_f32_layout<kLayoutGeneric>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+    return launch_f32_t<1, kLayoutDirbe, false>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  if (layout == 1) return launch_f32_layout<kLayoutDirbe>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  if (layout == 2) return launch_f32_layout<kLayoutPlanck>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  return launch_f32_layout<kLayoutGeneric>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
 }
 
 }  // namespace zl

@@ -143,7 +143,7 @@ __device__ __forceinline__ double density_f64(const ZlComponent& C, double X0, d
 template <int NSPEC>
 __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KParamsF64 P,
                                                       const double* __restrict__ u, int64_t n_pix,
-                                                      const ZlObserver* __restrict__ observers, int n_obs,
+                                                      const ObsArgs OA,
                                                       double* __restrict__ out_comps, double* __restrict__ out_total) {
   extern __shared__ double sm[];
   const int nT = P.m.n_temps;
@@ -166,8 +166,8 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
 
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
     const double ux = u[i], uy = u[n_pix + i], uz = u[2 * n_pix + i];
-    const ZlObserver& O = observers[find_observer(observers, n_obs, i)];
-    const double ox = O.obs[0], oy = O.obs[1], oz = O.obs[2];
+    const PixObs O = pixel_observer(OA, i, n_pix);
+    const double ox = O.ox, oy = O.oy, oz = O.oz;
     const uint32_t outside = O.outside;
 
     // line_of_sight.py:70-85
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
           }
           hs_len = sp - st;
         }
-        const double dens = density_f64(C, X0, X1, X2, O.earth[0], O.earth[1]);
+        const double dens = density_f64(C, X0, X1, X2, O.ex, O.ey);
         if (P.m.family == ZL_RRM) {  // brightness.py:80-83
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) acc[c][s] += bb[s] * dens * P.m.spec[s].calibration * 0.5 * hs_len * wk;
@@ -267,14 +267,14 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
 }
 
 template <int NSPEC>
-static cudaError_t launch_f64_t(const KParamsF64& P, const double* u, int64_t n, const ZlObserver* obs, int n_obs,
+static cudaError_t launch_f64_t(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
                                 double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
   const size_t smem = sizeof(double) * P.m.n_temps * (1 + 2 * NSPEC);
   int64_t blocks_needed = (n + tpb - 1) / tpb;
   int64_t grid = (int64_t)num_sms * bps;
   if (grid > blocks_needed) grid = blocks_needed;
   if (grid < 1) grid = 1;
-  fwd_f64_kernel<NSPEC><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, n_obs, oc, ot);
+  fwd_f64_kernel<NSPEC><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
   return cudaGetLastError();
 }
 
@@ -306,13 +306,13 @@ cudaError_t launch_density_grid(const ZlModel& M, const double* x, int nx, const
   return cudaGetLastError();
 }
 
-cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ZlObserver* obs, int n_obs,
+cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
                            double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
   switch (P.m.n_spec) {
-    case 1: return launch_f64_t<1>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-    case 2: return launch_f64_t<2>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-    case 3: return launch_f64_t<3>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
-    default: return launch_f64_t<4>(P, u, n, obs, n_obs, oc, ot, st, tpb, bps, num_sms);
+    case 1: return launch_f64_t<1>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 2: return launch_f64_t<2>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 3: return launch_f64_t<3>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    default: return launch_f64_t<4>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
   }
 }
 

@@ -172,3 +172,158 @@ def density_grid(zl_model: _lib.ZlModel, x_dev, y_dev, z_dev, earth_xyz, out=Non
     )
     _lib.check(rc, "zl_density_grid")
     return out
+
+
+def _soa3(x, n, dev, what):
+    torch = _torch()
+    if x is None:
+        return None
+    if not isinstance(x, torch.Tensor):
+        x = torch.from_numpy(np.ascontiguousarray(np.asarray(x, dtype=np.float64)))
+    x = x.to(device=dev, dtype=torch.float64)
+    if x.dim() == 1:
+        x = x.reshape(3, 1)
+    if x.shape[0] != 3 or x.shape[-1] not in (1, n):
+        raise ValueError(f"{what} must be (3,) or (3, {n})")
+    return x.expand(3, n).contiguous() if x.shape[-1] != n else x.contiguous()
+
+
+def forward_tod(zl_model, u_dev, obs_xyz, earth_xyz, precision, want_comps=True, want_total=True, out_comps=None,
+                out_total=None, flags=None, stream: int | None = None):
+    """Run ``zl_forward_tod``: one observer / Earth position per pixel ((3, N) each, device or host)."""
+    torch = _torch()
+    if u_dev.dtype != torch.float64 or not u_dev.is_cuda or u_dev.dim() != 2 or u_dev.shape[0] != 3:
+        raise ValueError("unit vectors must be a float64 CUDA tensor of shape (3, N)")
+    u_dev = u_dev.contiguous()
+    n, dev = u_dev.shape[1], u_dev.device
+    obs = _soa3(obs_xyz, n, dev, "observer positions")
+    earth = _soa3(earth_xyz, n, dev, "Earth positions")
+    ns, nc = zl_model.n_spec, zl_model.n_comps
+    if want_comps and out_comps is None:
+        out_comps = torch.empty((ns, nc, n), dtype=torch.float64, device=dev)
+    if want_total and out_total is None:
+        out_total = torch.empty((ns, n), dtype=torch.float64, device=dev)
+    if flags is None:
+        flags = torch.empty(1, dtype=torch.int32, device=dev)
+    rc = _lib.load().zl_forward_tod(
+        ctypes.byref(zl_model),
+        ctypes.c_void_p(u_dev.data_ptr()),
+        n,
+        ctypes.c_void_p(obs.data_ptr()),
+        ctypes.c_void_p(earth.data_ptr() if earth is not None else 0),
+        ctypes.c_void_p(flags.data_ptr()),
+        precision_code(precision),
+        ctypes.c_void_p(out_comps.data_ptr() if out_comps is not None else 0),
+        ctypes.c_void_p(out_total.data_ptr() if out_total is not None else 0),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(dev)),
+    )
+    _lib.check(rc, "zl_forward_tod")
+    return (out_comps if want_comps else None), (out_total if want_total else None)
+
+
+def backward_tod(zl_model, u_dev, obs_xyz, earth_xyz, g_comps=None, g_total=None, grad_out=None, workspace=None,
+                 flags=None, stream: int | None = None):
+    """Run ``zl_backward_tod``: gradient w.r.t. the parameter vector for time-ordered positions."""
+    torch = _torch()
+    if (g_comps is None) == (g_total is None):
+        raise ValueError("pass exactly one of g_comps (n_spec, C, N) or g_total (n_spec, N)")
+    u_dev = u_dev.contiguous()
+    n, dev = u_dev.shape[1], u_dev.device
+    obs = _soa3(obs_xyz, n, dev, "observer positions")
+    earth = _soa3(earth_xyz, n, dev, "Earth positions")
+    g = (g_comps if g_comps is not None else g_total).to(device=dev, dtype=torch.float64).contiguous()
+    want = (zl_model.n_spec, zl_model.n_comps, n) if g_comps is not None else (zl_model.n_spec, n)
+    if tuple(g.shape) != want:
+        raise ValueError(f"upstream gradient must have shape {want}, got {tuple(g.shape)}")
+    if grad_out is None:
+        grad_out = torch.empty(grad_count(zl_model), dtype=torch.float64, device=dev)
+    need = backward_workspace_bytes(zl_model, n)
+    if workspace is None or workspace.numel() * workspace.element_size() < need:
+        workspace = torch.empty(max(need, 8), dtype=torch.uint8, device=dev)
+    if flags is None:
+        flags = torch.empty(1, dtype=torch.int32, device=dev)
+    rc = _lib.load().zl_backward_tod(
+        ctypes.byref(zl_model),
+        ctypes.c_void_p(u_dev.data_ptr()),
+        n,
+        ctypes.c_void_p(obs.data_ptr()),
+        ctypes.c_void_p(earth.data_ptr() if earth is not None else 0),
+        ctypes.c_void_p(flags.data_ptr()),
+        ctypes.c_void_p(g.data_ptr() if g_comps is not None else 0),
+        ctypes.c_void_p(g.data_ptr() if g_total is not None else 0),
+        ctypes.c_void_p(grad_out.data_ptr()),
+        ctypes.c_void_p(workspace.data_ptr()),
+        workspace.numel() * workspace.element_size(),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(dev)),
+    )
+    _lib.check(rc, "zl_backward_tod")
+    return grad_out
+
+
+def spline_eval(knots_dev, coef_dev, t_dev, out=None, stream: int | None = None):
+    """Run ``zl_spline_eval``: (3, n) positions of a piecewise cubic (coef (4, K-1, 3)) at times t."""
+    torch = _torch()
+    k = knots_dev.numel()
+    if tuple(coef_dev.shape) != (4, k - 1, 3):
+        raise ValueError(f"coefficients must have shape (4, {k - 1}, 3)")
+    n = t_dev.numel()
+    if out is None:
+        out = torch.empty((3, n), dtype=torch.float64, device=t_dev.device)
+    rc = _lib.load().zl_spline_eval(
+        ctypes.c_void_p(knots_dev.data_ptr()),
+        k,
+        ctypes.c_void_p(coef_dev.data_ptr()),
+        ctypes.c_void_p(t_dev.data_ptr()),
+        n,
+        ctypes.c_void_p(out.data_ptr()),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(t_dev.device)),
+    )
+    _lib.check(rc, "zl_spline_eval")
+    return out
+
+
+def semb_l2(earth_dev, l2_distance: float, whole_array_norm: bool, out=None, stream: int | None = None):
+    """Run ``zl_semb_l2`` on (3, n) Earth positions."""
+    torch = _torch()
+    earth_dev = earth_dev.contiguous()
+    n = earth_dev.shape[1]
+    if out is None:
+        out = torch.empty_like(earth_dev)
+    scratch = torch.empty(_lib.ZL_SEMB_L2_SCRATCH, dtype=torch.float64, device=earth_dev.device)
+    rc = _lib.load().zl_semb_l2(
+        ctypes.c_void_p(earth_dev.data_ptr()),
+        n,
+        float(l2_distance),
+        1 if whole_array_norm else 0,
+        ctypes.c_void_p(scratch.data_ptr()),
+        scratch.numel(),
+        ctypes.c_void_p(out.data_ptr()),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(earth_dev.device)),
+    )
+    _lib.check(rc, "zl_semb_l2")
+    return out
+
+
+def directions(lon_dev, lat_dev, rotation=None, out=None, stream: int | None = None):
+    """Run ``zl_directions``: (3, n) ecliptic unit vectors of (lon, lat) [rad] under a 3x3 rotation."""
+    torch = _torch()
+    lon_dev, lat_dev = lon_dev.contiguous(), lat_dev.contiguous()
+    n = lon_dev.numel()
+    if lat_dev.numel() != n:
+        raise ValueError("lon and lat must have the same size")
+    if out is None:
+        out = torch.empty((3, n), dtype=torch.float64, device=lon_dev.device)
+    rot = None
+    if rotation is not None:
+        r = np.ascontiguousarray(np.asarray(rotation, dtype=np.float64).reshape(9))
+        rot = (ctypes.c_double * 9)(*r.tolist())
+    rc = _lib.load().zl_directions(
+        ctypes.c_void_p(lon_dev.data_ptr()),
+        ctypes.c_void_p(lat_dev.data_ptr()),
+        n,
+        rot,
+        ctypes.c_void_p(out.data_ptr()),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(lon_dev.device)),
+    )
+    _lib.check(rc, "zl_directions")
+    return out

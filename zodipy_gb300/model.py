@@ -167,6 +167,9 @@ class Model:
         if n_time > skycoord.size:
             raise ValueError("The size of obstime must be either 1 or ncoords.")
 
+        if n_time > 1:
+            emission = self._evaluate_tod(skycoord, obspos, obspos_isstr, obstime_mjd.reshape(-1), return_comps)
+            return self._as_output_quantity(emission, skycoord)
         earth_xyz = self._earth_position(obstime_mjd)
         if obspos_isstr:
             obs_xyz = self._body_position(obspos, obstime_mjd, earth_xyz)
@@ -227,6 +230,49 @@ class Model:
         return self._precision
 
     # -- internals -----------------------------------------------------------
+    def _evaluate_tod(self, skycoord, obspos, obspos_isstr, mjd, return_comps):
+        """Time-ordered call (``model.py:177-180,205-235``): positions from hourly splines on the device."""
+        import torch
+
+        from . import tod
+        from .ephemeris import MEAN_DIST_TO_L2
+
+        knots = tod.interp_obstimes(float(mjd[0]), float(mjd[-1]))
+        t_dev = torch.from_numpy(np.ascontiguousarray(mjd, dtype=np.float64)).cuda()
+        earth_knots = self._earth_position(knots)
+        earth_dev = tod.spline_positions(knots, earth_knots, t_dev)
+        if obspos_isstr:
+            body = obspos.lower()
+            if body == "earth":
+                obs_dev = earth_dev
+            elif body == "semb-l2":  # bodies.py:38-50 with the norm of the whole (3, n) array
+                obs_dev = engine.semb_l2(earth_dev, MEAN_DIST_TO_L2, whole_array_norm=True)
+            else:
+                obs_dev = tod.spline_positions(knots, self._body_position(body, knots, earth_knots), t_dev)
+        else:
+            try:
+                obs = np.asarray(as_quantity(obspos).to_value(AU), dtype=np.float64)
+            except UnitConversionError as error:
+                raise UnitConversionError("The observer position must be in length units.") from error
+            obs_dev = torch.from_numpy(np.ascontiguousarray(obs.reshape(3, -1))).cuda()
+        u_dev = self._unit_vectors_device(skycoord)
+        comps, total = engine.forward_tod(
+            self._zl_model, u_dev, obs_dev, earth_dev, self._precision, return_comps, not return_comps
+        )
+        res = comps[0] if return_comps else total[0]
+        return res.cpu().numpy()
+
+    @staticmethod
+    def _unit_vectors_device(skycoord):
+        """(3, N) ecliptic unit vectors on the device; a lite SkyCoord is rotated by ``zl_directions``."""
+        import torch
+
+        if isinstance(skycoord, _LiteSkyCoord):
+            lon = torch.from_numpy(np.ascontiguousarray(np.atleast_1d(skycoord.lon), dtype=np.float64)).cuda()
+            lat = torch.from_numpy(np.ascontiguousarray(np.atleast_1d(skycoord.lat), dtype=np.float64)).cuda()
+            return engine.directions(lon, lat, skycoord.ecliptic_rotation())
+        return torch.from_numpy(np.ascontiguousarray(Model._unit_vectors(skycoord))).cuda()
+
     def _earth_position(self, mjd: np.ndarray) -> np.ndarray:
         return earth_xyz(mjd, self._ephemeris)
 
@@ -283,18 +329,9 @@ class Model:
         if obs.shape[1] not in (1, n) or earth.shape[1] not in (1, n):
             raise ValueError("positions must be (3,) or (3, ncoords)")
         per_pixel = obs.shape[1] > 1 or earth.shape[1] > 1
-        if per_pixel:
-            # time-ordered input: one observer record per pixel, cutoff flags OR-ed
-            # over the call (line_of_sight.py:72 tests `.any()` over all positions)
-            n_rec = n
-            obs = np.broadcast_to(obs, (3, n))
-            earth = np.broadcast_to(earth, (3, n))
-            pix_begin = np.arange(n, dtype=np.int64)
-        else:
-            n_rec = 1
-            pix_begin = np.zeros(1, dtype=np.int64)
-        table = packing.observer_table(self._zl_model, obs, earth, pix_begin, any_mode=per_pixel)
-        obs_dev = engine.upload_observers(table)
+        if not per_pixel:
+            table = packing.observer_table(self._zl_model, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
+            obs_dev = engine.upload_observers(table)
         if on_device:
             u_dev = unit_vectors.to(torch.float64).contiguous()
         else:
@@ -305,7 +342,12 @@ class Model:
             if not u_host.is_pinned():
                 u_host = u_host.pin_memory()
             u_dev = u_host.to("cuda", non_blocking=True)
-        comps, total = engine.forward(self._zl_model, u_dev, obs_dev, n_rec, prec, return_comps, not return_comps)
+        if per_pixel:
+            # time-ordered input: positions per pixel, cutoff flags OR-ed over the call on the
+            # device (line_of_sight.py:72 tests `.any()` over all positions)
+            comps, total = engine.forward_tod(self._zl_model, u_dev, obs, earth, prec, return_comps, not return_comps)
+        else:
+            comps, total = engine.forward(self._zl_model, u_dev, obs_dev, 1, prec, return_comps, not return_comps)
         res = comps[0] if return_comps else total[0]
         if on_device:
             return res
