@@ -195,3 +195,17 @@ def test_rrm_parameters_round_trip_and_adjoint_refusal(lib):
     assert m.zl_model.comp[2].range == m.zl_model.comp[3].range == m.zl_model.comp[4].range
     with pytest.raises(_lib.ZodiGBError, match="Kelsall"):
         engine.grad_count(m.zl_model)
+
+
+def test_model_set_rejects_incompatible_models(lib):
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import units as u
+
+    with pytest.raises(TypeError):
+        zg.ModelSet([])
+    with pytest.raises(ValueError):
+        zg.ModelSet([zg.Model(25 * u.micron), zg.Model(857 * u.GHz, name="planck18")])
+    with pytest.raises(ValueError):
+        zg.ModelSet([zg.Model(25 * u.micron), zg.Model(12 * u.micron, gauss_quad_degree=20)])
+    s = zg.ModelSet([zg.Model(x * u.micron) for x in (1.25, 12, 25, 60, 100)])
+    assert len(s) == 5 and [z.n_spec for z in s._zls] == [4, 1]

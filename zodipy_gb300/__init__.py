@@ -7,8 +7,9 @@ the per-pixel quadrature running in libzodigb (``include/zodigb.h``).
 
 from . import units
 from .coords import SkyCoord, Time
+from .fused import ModelSet
 from .model import Model
 from .number_density import grid_number_density
 from .zodiacal_light_model import model_registry
 
-__all__ = ("Model", "grid_number_density", "model_registry", "units", "SkyCoord", "Time")
+__all__ = ("Model", "ModelSet", "grid_number_density", "model_registry", "units", "SkyCoord", "Time")

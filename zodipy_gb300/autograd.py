@@ -14,6 +14,7 @@ import numpy as np
 import torch
 
 from . import _lib, engine, packing, params
+from .fused import fuse_models  # noqa: F401  (one ZlModel for several spectral sets)
 
 
 class _Emission(torch.autograd.Function):
@@ -87,23 +88,3 @@ class ZodiAdjoint:
         return _Emission.apply(theta, self, return_comps)
 
 
-def fuse_models(models) -> _lib.ZlModel:
-    """One ``ZlModel`` evaluating several ``Model``s that share geometry in one launch.
-
-    The models must come from the same registry entry and quadrature degree;
-    they may differ in wavelength / bandpass (each keeps its own blackbody
-    table and spectral parameters).
-    """
-    first = models[0]
-    for m in models[1:]:
-        if m._ipd_model is not first._ipd_model and m.get_parameters()["comps"] != first.get_parameters()["comps"]:
-            raise ValueError("fused models must share their components")
-        if m._gauss_quad_degree != first._gauss_quad_degree:
-            raise ValueError("fused models must share the quadrature degree")
-    return packing.pack_model(
-        first._ipd_model,
-        [m._spectrum for m in models],
-        [m._b_nu_table for m in models],
-        first._quad_points,
-        first._quad_weights,
-    )

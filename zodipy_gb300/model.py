@@ -150,6 +150,10 @@ class Model:
     # -- public API -----------------------------------------------------------
     def evaluate(self, skycoord, *, obspos="earth", return_comps: bool = False, nprocesses: int = 1):
         """Zodiacal emission [MJy/sr] toward every coordinate (``model.py:119-203``)."""
+        return self._as_output_quantity(self._evaluate_sky(skycoord, obspos, return_comps), skycoord)
+
+    def _evaluate_sky(self, skycoord, obspos, return_comps, zl=None, all_spec=False, precision=None):
+        """Validation and dispatch of ``evaluate``; ``zl`` / ``all_spec`` serve fused model sets."""
         try:
             if skycoord.obstime is None:
                 raise ValueError("The `obstime` attribute of the `SkyCoord` object is not set.")
@@ -168,8 +172,9 @@ class Model:
             raise ValueError("The size of obstime must be either 1 or ncoords.")
 
         if n_time > 1:
-            emission = self._evaluate_tod(skycoord, obspos, obspos_isstr, obstime_mjd.reshape(-1), return_comps)
-            return self._as_output_quantity(emission, skycoord)
+            return self._evaluate_tod(
+                skycoord, obspos, obspos_isstr, obstime_mjd.reshape(-1), return_comps, zl, all_spec, precision
+            )
         earth_xyz = self._earth_position(obstime_mjd)
         if obspos_isstr:
             obs_xyz = self._body_position(obspos, obstime_mjd, earth_xyz)
@@ -179,8 +184,8 @@ class Model:
             except UnitConversionError as error:
                 raise UnitConversionError("The observer position must be in length units.") from error
         unit_vectors = self._unit_vectors(skycoord)
-        emission = self._evaluate(unit_vectors, np.asarray(obs_xyz, dtype=np.float64), earth_xyz, return_comps)
-        return self._as_output_quantity(emission, skycoord)
+        obs_xyz = np.asarray(obs_xyz, dtype=np.float64)
+        return self._evaluate(unit_vectors, obs_xyz, earth_xyz, return_comps, precision, zl=zl, all_spec=all_spec)
 
     def evaluate_xyz(self, unit_vectors, obs_pos, earth_pos=None, *, return_comps: bool = False, precision=None, out=None):
         """The ``_evaluate`` seam on explicit heliocentric-ecliptic vectors.
@@ -230,7 +235,7 @@ class Model:
         return self._precision
 
     # -- internals -----------------------------------------------------------
-    def _evaluate_tod(self, skycoord, obspos, obspos_isstr, mjd, return_comps):
+    def _evaluate_tod(self, skycoord, obspos, obspos_isstr, mjd, return_comps, zl=None, all_spec=False, precision=None):
         """Time-ordered call (``model.py:177-180,205-235``): positions from hourly splines on the device."""
         import torch
 
@@ -256,11 +261,11 @@ class Model:
                 raise UnitConversionError("The observer position must be in length units.") from error
             obs_dev = torch.from_numpy(np.ascontiguousarray(obs.reshape(3, -1))).cuda()
         u_dev = self._unit_vectors_device(skycoord)
-        comps, total = engine.forward_tod(
-            self._zl_model, u_dev, obs_dev, earth_dev, self._precision, return_comps, not return_comps
-        )
-        res = comps[0] if return_comps else total[0]
-        return res.cpu().numpy()
+        zl = self._zl_model if zl is None else zl
+        prec = self._precision if precision is None else engine.precision_code(precision)
+        comps, total = engine.forward_tod(zl, u_dev, obs_dev, earth_dev, prec, return_comps, not return_comps)
+        res = comps if return_comps else total
+        return (res if all_spec else res[0]).cpu().numpy()
 
     @staticmethod
     def _unit_vectors_device(skycoord):
@@ -314,9 +319,11 @@ class Model:
         _, u = _astropy()
         return emission << (u.MJy / u.sr)
 
-    def _evaluate(self, unit_vectors, obs_xyz, earth_xyz, return_comps, precision=None, out=None):
+    def _evaluate(self, unit_vectors, obs_xyz, earth_xyz, return_comps, precision=None, out=None, zl=None,
+                  all_spec=False):
         import torch
 
+        zl = self._zl_model if zl is None else zl
         prec = self._precision if precision is None else engine.precision_code(precision)
         on_device = isinstance(unit_vectors, torch.Tensor) and unit_vectors.is_cuda
         n = unit_vectors.shape[-1]
@@ -330,7 +337,7 @@ class Model:
             raise ValueError("positions must be (3,) or (3, ncoords)")
         per_pixel = obs.shape[1] > 1 or earth.shape[1] > 1
         if not per_pixel:
-            table = packing.observer_table(self._zl_model, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
+            table = packing.observer_table(zl, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
             obs_dev = engine.upload_observers(table)
         if on_device:
             u_dev = unit_vectors.to(torch.float64).contiguous()
@@ -345,10 +352,12 @@ class Model:
         if per_pixel:
             # time-ordered input: positions per pixel, cutoff flags OR-ed over the call on the
             # device (line_of_sight.py:72 tests `.any()` over all positions)
-            comps, total = engine.forward_tod(self._zl_model, u_dev, obs, earth, prec, return_comps, not return_comps)
+            comps, total = engine.forward_tod(zl, u_dev, obs, earth, prec, return_comps, not return_comps)
         else:
-            comps, total = engine.forward(self._zl_model, u_dev, obs_dev, 1, prec, return_comps, not return_comps)
-        res = comps[0] if return_comps else total[0]
+            comps, total = engine.forward(zl, u_dev, obs_dev, 1, prec, return_comps, not return_comps)
+        res = comps if return_comps else total
+        if not all_spec:
+            res = res[0]
         if on_device:
             return res
         if out is None:
