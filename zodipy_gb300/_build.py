@@ -17,7 +17,18 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libzodigb.so")
-SOURCES = ["zl_api.cu", "zl_fwd_f64.cu", "zl_fwd_f32.cu", "zl_bwd_f32.cu", "zl_diag.cu", "zl_static.cu", "zl_tod.cu"]
+SOURCES = [
+    "zl_api.cu",
+    "zl_fwd_f64.cu",
+    "zl_fwd_f32.cu",
+    "zl_fwd_f32_dirbe.cu",
+    "zl_fwd_f32_planck.cu",
+    "zl_fwd_f32_generic.cu",
+    "zl_bwd_f32.cu",
+    "zl_diag.cu",
+    "zl_static.cu",
+    "zl_tod.cu",
+]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

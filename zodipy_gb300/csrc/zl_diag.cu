@@ -5,6 +5,8 @@
 // the benchmark measures both with these kernels on the same GPU and clock:
 //  - which = 0: ex2.approx.ftz.f32 (one MUFU op each), 8 independent chains per thread
 //  - which = 1: fma.rn.f32 (one FFMA each), 8 independent chains per thread
+//  - which = 2: packed fma.rn.f32x2 (two FMAs each), 8 independent float2 chains per thread;
+//    counted in FMAs, so it shows whether a packed instruction doubles the FP32 rate
 // Every result feeds a store guarded by an impossible condition so the chains
 // are not removed.
 #include <cuda_runtime.h>
@@ -46,11 +48,26 @@ __global__ void __launch_bounds__(256) fma_probe(float* sink, int iters, float s
   if (s == 1234.5f) sink[blockIdx.x] = s;
 }
 
+__global__ void __launch_bounds__(256) fma2_probe(float* sink, int iters, float seed) {
+  float2 a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = make_float2(seed + (float)(threadIdx.x + j), seed - (float)j);
+  const float2 m = make_float2(0.999999f, 0.999998f), c = make_float2(1e-7f, 2e-7f);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = __ffma2_rn(a[j], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j].x + a[j].y;
+  if (s == 1234.5f) sink[blockIdx.x] = s;
+}
+
 }  // namespace
 
 extern "C" ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int32_t sink_len,
                                          double* ops_per_launch, void* stream) {
-  if ((which != 0 && which != 1) || iters < 1 || !sink_dev || !ops_per_launch) return ZL_ERR_ARG;
+  if (which < 0 || which > 2 || iters < 1 || !sink_dev || !ops_per_launch) return ZL_ERR_ARG;
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return ZL_ERR_CUDA;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ZL_ERR_CUDA;
@@ -59,9 +76,11 @@ extern "C" ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* si
   cudaStream_t st = (cudaStream_t)stream;
   if (which == 0)
     xu_probe<<<blocks, 256, 0, st>>>(sink_dev, iters, 1.0f);
-  else
+  else if (which == 1)
     fma_probe<<<blocks, 256, 0, st>>>(sink_dev, iters, 1.0f);
+  else
+    fma2_probe<<<blocks, 256, 0, st>>>(sink_dev, iters, 1.0f);
   if (cudaGetLastError() != cudaSuccess) return ZL_ERR_CUDA;
-  *ops_per_launch = (double)blocks * 256.0 * 8.0 * (double)iters;
+  *ops_per_launch = (double)blocks * 256.0 * 8.0 * (double)iters * (which == 2 ? 2.0 : 1.0);
   return ZL_OK;
 }

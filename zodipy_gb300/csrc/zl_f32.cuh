@@ -30,6 +30,12 @@ struct Lay {
       if (first(j)) ++r;
     return r;
   }
+  // first band of component c's range (c itself if none precedes it)
+  __host__ __device__ static constexpr int first_band(int c) {
+    for (int j = 0; j < c; ++j)
+      if (range(j) == range(c) && type(j) == ZL_BAND) return j;
+    return c;
+  }
 };
 
 // Root of |obs + s u| = cutoff (line_of_sight.py:80-85) in float-float; b omits

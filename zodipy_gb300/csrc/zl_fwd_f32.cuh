@@ -1,0 +1,354 @@
+// Fast forward kernel: the line-of-sight integrand in float32 on the FP32/MUFU pipes
+// (Kelsall, zodipy/brightness.py:21-56; RRM, zodipy/brightness.py:59-83, through the
+// generic layout).
+//
+// Same integral as the float64 kernel (zodipy/model.py:253-277); what changes is
+// the arithmetic, chosen for GB300 where FP64 runs at a small fraction of FP32:
+//  - the cutoff-sphere intersections (zodipy/line_of_sight.py:64-85) are solved
+//    per pixel in float-float (~48-bit) arithmetic;
+//  - for the ring and the feature (zodipy/number_density.py:113-181), whose
+//    radial profiles are narrow (sigma_r = 0.025 AU), R^2 - R0^2 at each node is
+//    w^2 + c' with w = R_los + u.(X_obs - X_0) carried in float-float and c' a
+//    per-pixel float-float constant, and R - R0 is recovered from it with one
+//    Newton step, so the Gaussian exponent keeps float32 relative accuracy;
+//  - heights above each symmetry plane are linear in the node abscissa with
+//    float-float per-pixel coefficients, evaluated to ~1 ulp with one FMA on
+//    the high parts plus first-order low-part corrections;
+//  - distances are never formed from the position vector: |X - X_0|^2 =
+//    w^2 + b^2 with w = R_los + u.(X_obs - X_0) (linear in the node abscissa,
+//    evaluated as above) and b^2 the squared impact parameter (a per-pixel
+//    constant), two non-negative terms, so lines of sight that graze the Sun
+//    keep float32 relative accuracy where R^-alpha is steepest;
+//  - everything else runs in float32 with single MUFU instructions (ex2, lg2,
+//    rsqrt), integer powers by squaring and 1 - e^-y by its series where it
+//    would cancel;
+//  - each component's quadrature sum is Kahan-compensated in float32 and
+//    written as float64.
+// One thread integrates one pixel over all nodes and components in node order,
+// so a pixel's result never depends on how pixels are partitioned.
+#pragma once
+
+#include "zl_f32.cuh"
+
+namespace zl {
+
+// Compile-time properties of a model for the built-in layouts (FLAGS); bit 0 set = read them
+// from the parameter block at run time instead (any model, the generic layout):
+//   bit 1        some component scatters sunlight (albedo != 0)
+//   bit 8 + c    component c is offset from the Sun
+//   bit 16 + c   band c has p == 4 (its (zeta/dzeta)^p is a square of a square)
+//   bit 24 + c   band c reuses the first band's 1 - e^-(R/delta_r)^20 (equal delta_r and offset)
+constexpr uint32_t kFlagsRuntime = 1u;
+
+template <uint32_t F>
+struct KFlags {
+  static constexpr bool runtime = (F & 1u) != 0;
+  __device__ static __forceinline__ bool scat(const KParamsF32& P) {
+    return runtime ? P.has_scat != 0 : ((F >> 1) & 1u) != 0;
+  }
+  __device__ static __forceinline__ bool offset(const KCompF32& C, int c) {
+    return runtime ? C.zero_offset == 0 : ((F >> (8 + c)) & 1u) != 0;
+  }
+  __device__ static __forceinline__ bool p4(const KCompF32& C, int c) {
+    return runtime ? C.c[5] != 0.f : ((F >> (16 + c)) & 1u) != 0;
+  }
+  __device__ static __forceinline__ bool share_first(int c) { return ((F >> (24 + c)) & 1u) != 0; }
+};
+
+template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
+__global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
+                                                      const double* __restrict__ u, int64_t n_pix,
+                                                      const ObsArgs OA,
+                                                      double* __restrict__ out_comps, double* __restrict__ out_total) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
+  constexpr int NC = L::ncomp();
+  extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
+  const int nT = P.n_temps;
+  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  __syncthreads();
+
+  const int nc = L::generic ? P.n_comps : NC;
+  const int nr = P.n_ranges;
+
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
+    // ---- per-pixel set-up -------------------------------------------------
+    const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+    const PixObs O = pixel_observer(OA, i, n_pix);
+    const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
+    const uint32_t outside = O.outside;
+    const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
+    const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
+
+    const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+    const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+    const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));  // u . X_obs
+
+    ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
+#pragma unroll
+    for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+      if (r < nr) {
+        const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
+                                                  : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
+        const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
+                                                      : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
+        hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+        mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+      } else {
+        hs_r[r] = ff{0.f, 0.f};
+        mid_r[r] = ff{0.f, 0.f};
+      }
+    }
+
+    // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
+    const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
+    const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
+    // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
+    const float bperp = Fl::scat(P) ? sqrtf(b2h) : 0.f;
+
+    // per-component set-up
+    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], wm_c[NC], cw_c[NC], mh_c[NC];
+    float b2_c[NC], fx1[NC], fx0[NC], fy1[NC], fy0[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (c >= nc) break;
+      const KCompF32& C = P.comp[c];
+      const int type = L::generic ? C.type : L::type(c);
+      ff hs = {0.f, 0.f}, md = {0.f, 0.f};
+      if (!L::generic) {
+        hs = hs_r[L::range(c)];
+        md = mid_r[L::range(c)];
+      } else {
+#pragma unroll
+        for (int r = 0; r < ZL_MAX_RANGES; ++r)
+          if (r == C.range) {
+            hs = hs_r[r];
+            md = mid_r[r];
+          }
+      }
+      hs_c[c] = hs;
+      mid_c[c] = md;
+      mh_c[c] = ff_add(md, beta_h);  // R_los + u . X_obs = hs x + mh
+      const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
+               dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+      // height above the symmetry plane, linear in the node abscissa x:
+      //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
+      const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+      z1_c[c] = ff_mul(hs, un);
+      z0_c[c] = ff_add(ff_mul(md, un), on);
+      // |X - X_0|^2 = w^2 + b^2,  w = hs x + (mid + beta),  beta = u . (X_obs - X_0),
+      // b^2 = |X_obs - X_0|^2 - beta^2;  the ring/feature use w^2 + c' with c' = b^2 - R0^2
+      wm_c[c] = mh_c[c];
+      b2_c[c] = b2h;
+      cw_c[c] = ff{0.f, 0.f};
+      if (Fl::offset(C, c) || (PRECISE && ringlike(type)) || masked(type)) {
+        const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
+        const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+        const ff bb = ff_add(d2, ff_neg(ff_mul(beta, beta)));
+        wm_c[c] = ff_add(md, beta);
+        b2_c[c] = fmaxf(bb.hi + bb.lo, 0.f);
+        cw_c[c] = masked(type) ? bb : ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
+      }
+      fx1[c] = fx0[c] = fy1[c] = fy0[c] = 0.f;
+      if (featurelike(type)) {
+        // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
+        // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
+        // two coordinates that are linear in the node abscissa
+        const float phi = atan2f((float)(O.ey - (double)C.oy), (float)(O.ex - (double)C.ox)) + C.c[6];
+        float sp, cp;
+        sincosf(phi, &sp, &cp);
+        const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+        const float rux = cp * uxf + sp * uyf, ruy = cp * uyf - sp * uxf;
+        const float rox = cp * ocx + sp * ocy, roy = cp * ocy - sp * ocx;
+        const float h = hs.hi + hs.lo, m = md.hi + md.lo;
+        fx1[c] = h * rux;
+        fx0[c] = fmaf(m, rux, rox);
+        fy1[c] = h * ruy;
+        fy0[c] = fmaf(m, ruy, roy);
+      }
+    }
+
+    float acc_s[NC][NSPEC], acc_c[NC][NSPEC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) {
+        acc_s[c][s] = 0.f;
+        acc_c[c][s] = 0.f;
+      }
+
+    // ---- quadrature nodes ------------------------------------------------
+#pragma unroll 1
+    for (int k = 0; k < P.n_nodes; ++k) {
+      const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
+      const float wk = P.gl_w[k];
+      float wh = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
+      float B[NSPEC], sf[NSPEC], t4s[NC];
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) {
+        B[s] = 0.f;
+        sf[s] = 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        t4s[c] = 0.f;
+        if (c >= nc) break;
+        const KCompF32& C = P.comp[c];
+        const int type = L::generic ? C.type : L::type(c);
+        const bool first = L::generic ? (C.first_in_range != 0) : L::first(c);
+        const bool precise = PRECISE && ringlike(type);
+        if (first) {
+          // brightness.py:27-33 — heliocentric distance of the node, R^2 = w^2 + b^2, and temperature
+          wh = lin_ff(hs_c[c], xk, mh_c[c]);
+          R2 = fmaf(wh, wh, b2h);
+          rinv = rsqrt_ftz(R2);
+          // one Newton step where 1/R feeds the bands' e^-(zeta/dzeta)^6 (sensitivity 6 x^6);
+          // the ring/feature distance is corrected from R^2 - R0^2 below instead
+          if (type == ZL_CLOUD || type == ZL_BAND || masked(type)) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
+          R = R2 * rinv;
+          lg2R = lg2_ftz(R);
+          const float T = (L::generic ? C.T0 : P.T0) * ex2_ftz((L::generic ? C.neg_delta : P.neg_delta) * lg2R);  // blackbody.py:16-30
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) B[s] = bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
+          if (Fl::scat(P)) {  // scattering.py:11-59
+            const float theta = atan2f(bperp, -wh);
+            const float flux = rinv * rinv;
+#pragma unroll
+            for (int s = 0; s < NSPEC; ++s) {
+              const KSpecF32& S = P.spec[s];
+              sf[s] = S.S * flux * (S.N * (S.C1 + S.C2 * theta + ex2_ftz(S.C3l2e * theta)));
+            }
+          }
+        }
+        // own distance when the component is offset from the Sun
+        float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R;
+        if (Fl::offset(C, c)) {
+          const float wc = lin_ff(hs_c[c], xk, wm_c[c]);
+          Rc2 = fmaf(wc, wc, b2_c[c]);
+          rcinv = rsqrt_ftz(Rc2);
+          if (type == ZL_BAND || masked(type)) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
+          Rc = Rc2 * rcinv;
+          lg2Rc = 0.5f * lg2_ftz(Rc2);
+        }
+        const float Z = lin_ff(z1_c[c], xk, z0_c[c]);
+        float dens;
+        if (type == ZL_CLOUD) {  // number_density.py:60-73
+          const float zeta = fabsf(Z) * rcinv;
+          const float g = zeta < C.c[4] ? zeta * zeta * C.c[5] : zeta - C.c[6];
+          const float gg = ex2_ftz(C.c[3] * lg2_ftz(g));
+          dens = C.c[0] * ex2_ftz(-C.c[1] * lg2Rc - C.c[2] * gg);
+        } else if (type == ZL_BAND) {  // number_density.py:99-110
+          const float zz = fabsf(Z) * rcinv * C.c[1];
+          const float z2 = zz * zz;
+          const float t2 = ex2_ftz(-kLog2e * (z2 * z2 * z2));
+          const float zp = Fl::p4(C, c) ? z2 * z2 : ex2_ftz(C.c[3] * lg2_ftz(zz));
+          const float t3 = fmaf(zp, C.c[2], 1.0f);
+          float t4 = 0.f;
+          bool shared = false;
+          if (Fl::runtime) {
+#pragma unroll
+            for (int j = 0; j < NC; ++j)
+              if (j < c && C.share_t4 == j) {
+                t4 = t4s[j];
+                shared = true;
+              }
+          } else if (Fl::share_first(c)) {
+            t4 = t4s[L::first_band(c)];
+            shared = true;
+          }
+          if (!shared) {
+            const float q = Rc2 * C.c[4];  // (R/delta_r)^2
+            const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+            const float y = q8 * q2;  // (R/delta_r)^20
+            // 1 - e^-y; below 1/4 by its series (relative error < 1e-7) instead of a cancelling difference
+            t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
+                           : 1.0f - ex2_ftz(-kLog2e * y);
+          }
+          t4s[c] = t4;
+          dens = C.c[0] * rcinv * t2 * t3 * t4;
+        } else if (ringlike(type)) {  // ring (number_density.py:136-139) and feature (:167-181), RRM: x A
+          float dR = Rc - C.c[1];
+          if (precise) {
+            // R^2 - R0^2 = w^2 + c' to ~1 ulp; one Newton step on R
+            const float D2 = sq_plus_ff(lin_ff2(hs_c[c], xk, wm_c[c]), cw_c[c]);
+            dR = dR + (D2 - dR * (Rc + C.c[1])) * (0.5f * rcinv);
+          }
+          float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
+          if (featurelike(type)) {
+            const float dth = atan2f(fmaf(fy1[c], xk.hi, fy0[c]), fmaf(fx1[c], xk.hi, fx0[c]));
+            arg = fmaf(dth * dth, C.c[7], arg);
+          }
+          dens = C.c[0] * ex2_ftz(-arg);
+        } else if (type == ZL_INTERSTELLAR) {  // number_density.py:259-264
+          dens = C.c[0];
+        } else {
+          dens = rrm_masked_density(C, type, hs_c[c], xk, wm_c[c], cw_c[c], z1_c[c], z0_c[c], Z, rcinv, lg2Rc);
+        }
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) {
+          const KSpecF32& S = P.spec[s];
+          float e = S.em1[c] * B[s];
+          if (Fl::scat(P)) e = fmaf(S.alb[c], sf[s], e);
+          kahan_add(acc_s[c][s], acc_c[c][s], wk * (e * dens));
+        }
+      }
+    }
+
+    // ---- outputs: x (stop - start)/2, component order total ----------------
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) {
+      double tot = 0.0;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c >= nc) break;
+        // explicit roundings: the total must equal the sum of the stored components bit for bit
+        const double v = __dmul_rn(__dsub_rn((double)acc_s[c][s], (double)acc_c[c][s]),
+                                   __dadd_rn((double)hs_c[c].hi, (double)hs_c[c].lo));
+        if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + i] = v;
+        tot = (c == 0) ? v : __dadd_rn(tot, v);
+      }
+      if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
+    }
+  }
+}
+
+template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
+static cudaError_t launch_f32_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
+                                double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+  const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
+  const int64_t blocks_needed = (n + tpb - 1) / tpb;
+  int64_t grid = (int64_t)num_sms * bps;
+  if (grid > blocks_needed) grid = blocks_needed;
+  if (grid < 1) grid = 1;
+  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE, FLAGS><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
+  return cudaGetLastError();
+}
+
+// One layout and flag set, every supported number of spectral sets.
+template <uint32_t LAYOUT, uint32_t FLAGS>
+static cudaError_t launch_f32_flags(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
+                                    double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+  switch (P.n_spec) {
+    case 1: return launch_f32_t<1, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 2: return launch_f32_t<2, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 3: return launch_f32_t<3, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    default: return launch_f32_t<4, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  }
+}
+
+// The flag set of the built-in Kelsall models (cloud offset, bands with p = 4, band 3 reusing
+// band 1's inner-cutoff term) for the DIRBE and Planck layouts.
+constexpr uint32_t kFlagsKelsall = (1u << 8) | (7u << 17) | (1u << 27);
+
+// Per-layout launchers (zl_fwd_f32_dirbe.cu, zl_fwd_f32_planck.cu, zl_fwd_f32_generic.cu).
+cudaError_t launch_fwd_f32_dirbe(const KParamsF32& P, uint32_t flags, bool plain_geometry, const double* u, int64_t n,
+                                 const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+                                 int num_sms);
+cudaError_t launch_fwd_f32_planck(const KParamsF32& P, uint32_t flags, const double* u, int64_t n, const ObsArgs& obs,
+                                  double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
+cudaError_t launch_fwd_f32_generic(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
+                                   double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
+
+}  // namespace zl
