@@ -25,6 +25,8 @@ SOURCES = [
     "zl_fwd_f32_planck.cu",
     "zl_fwd_f32_generic.cu",
     "zl_bwd_f32.cu",
+    "zl_bwd_f32_dirbe.cu",
+    "zl_bwd_f32_planck.cu",
     "zl_diag.cu",
     "zl_static.cu",
     "zl_tod.cu",

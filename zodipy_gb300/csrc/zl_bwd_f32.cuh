@@ -1,0 +1,482 @@
+// Adjoint (reverse-mode) kernel: gradient of a per-pixel loss with respect to
+// every model parameter, recomputing the integrand instead of storing
+// pixels x nodes x components.
+//
+// For out[s, c, i] = hs_c(i) * sum_k w_k e_sc(X_ik) n_c(X_ik)
+// (zodipy/brightness.py:21-56 summed as zodipy/line_of_sight.py:55-61) and an
+// upstream gradient g[s, c, i] = dL/d out[s, c, i], each thread evaluates one
+// pixel and accumulates, per node,
+//   dL/dp += sum_s g[s,c] hs w * d(e_sc n_c)/dp
+// with analytic derivatives of the Kelsall-98 densities
+// (zodipy/number_density.py:47-181), of T(R) = T0 R^-delta through the
+// blackbody table's segment slope (numpy.interp's derivative; 0 where it
+// clamps), and of the scattering term (zodipy/scattering.py:34-59).  All
+// spectral sets of a fused model share one pass: geometry and densities are
+// evaluated once per node and weighted by E_c = sum_s g[s,c] e_sc.
+//
+// Parameters follow the reference's parameter dictionary
+// (zodipy/zodiacal_light_model.py:38-55): per component, in order,
+// x_0, y_0, z_0, i, Omega, n_0 and the type's own (cloud: alpha, beta, gamma,
+// mu; band: delta_zeta, v, p, delta_r; ring: R, sigma_r, sigma_z; feature:
+// R, sigma_r, sigma_z, theta, sigma_theta) with angles in degrees; then T_0,
+// delta; then per spectral set the interpolated emissivity[c], albedo[c], C1,
+// C2, C3 and solar irradiance.
+//
+// Determinism: pixels are cut into fixed 128-pixel tiles; one block reduces a
+// tile with a fixed shuffle tree and writes its partial vector to
+// partials[tile]; a second kernel sums the tiles in a fixed order.  The result
+// depends neither on the grid size nor on which SM ran which tile.
+#pragma once
+
+#include "zl_f32.cuh"
+
+namespace zl {
+
+constexpr float kLn2 = 0.6931471805599453f;
+constexpr float kDeg = 0.017453292519943295f;  // d(rad)/d(deg)
+constexpr int kTile = 128;
+
+template <uint32_t LAYOUT, int NSPEC>
+struct GradLay {
+  using L = Lay<LAYOUT>;
+  static constexpr int NC = L::ncomp();
+  __host__ __device__ static constexpr int npar(int t) {
+    return t == ZL_CLOUD ? 10 : (t == ZL_BAND ? 10 : (t == ZL_RING ? 9 : 11));
+  }
+  __host__ __device__ static constexpr int off(int c) {
+    int o = 0;
+    for (int j = 0; j < c; ++j) o += npar(L::type(j));
+    return o;
+  }
+  static constexpr int NCP = off(NC);
+  static constexpr int T0 = NCP, DELTA = NCP + 1;
+  static constexpr int PER_SPEC = 2 * NC + 4;
+  __host__ __device__ static constexpr int spec0(int s) { return NCP + 2 + s * PER_SPEC; }
+  __host__ __device__ static constexpr int eps(int c, int s) { return spec0(s) + c; }
+  __host__ __device__ static constexpr int alb(int c, int s) { return spec0(s) + NC + c; }
+  __host__ __device__ static constexpr int C(int j, int s) { return spec0(s) + 2 * NC + j; }  // C1, C2, C3, S
+  static constexpr int NG = NCP + 2 + NSPEC * PER_SPEC;
+};
+
+// True when component c is the last component of its LOS range among those in MASK.
+template <uint32_t LAYOUT, uint32_t MASK>
+__host__ __device__ constexpr bool last_of_range(int c) {
+  for (int j = c + 1; j < Lay<LAYOUT>::ncomp(); ++j)
+    if ((MASK >> j) & 1u) return Lay<LAYOUT>::range(j) != Lay<LAYOUT>::range(c);
+  return true;
+}
+
+// MASK selects the components this launch differentiates (bit c = component c).
+// A model's components are split into groups that each own their LOS ranges, so
+// every group launch carries only its own accumulators; parameters shared by
+// all components (T_0, delta, C1..C3, S) are summed over the groups' partials.
+// SCAT: some component has a non-zero albedo (scattering terms are evaluated).
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
+__global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ KParamsF32 P,
+                                                        const __grid_constant__ KGradAux A,
+                                                        const double* __restrict__ u, int64_t n_pix,
+                                                        const ObsArgs OA,
+                                                        const double* __restrict__ g_comps,
+                                                        const double* __restrict__ g_total,
+                                                        double* __restrict__ partials, int64_t n_tiles) {
+  using L = Lay<LAYOUT>;
+  using G = GradLay<LAYOUT, NSPEC>;
+  using Fl = KFlags<FLAGS>;
+  constexpr int NC = L::ncomp();
+  constexpr int NG = G::NG;
+  __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
+  __shared__ float red_sm[kTile / 32][NG];
+  const int nT = P.n_temps;
+  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  __syncthreads();
+  const int nr = P.n_ranges;
+
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t i = tile * kTile + threadIdx.x;
+    float acc[NG];
+#pragma unroll
+    for (int j = 0; j < NG; ++j) acc[j] = 0.f;
+
+    if (i < n_pix) {
+      // ---- per-pixel set-up (as the forward kernel) ---------------------------
+      const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+      const PixObs O = pixel_observer(OA, i, n_pix);
+      const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
+      const uint32_t outside = O.outside;
+      const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
+      const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
+      const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+      const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+      const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));
+      ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
+#pragma unroll
+      for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+        bool used = false;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
+        if (used && r < nr) {
+          const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
+                                                    : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
+          const ff sp = ((outside >> (2 * r + 1)) & 1u)
+                            ? ff{(float)kEps, 0.f}
+                            : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
+          hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+          mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+        } else {
+          hs_r[r] = mid_r[r] = ff{0.f, 0.f};
+        }
+      }
+      float bperp = 0.f;
+      if (SCAT) {
+        const float cx = uyf * ozf - uzf * oyf, cy = uzf * oxf - uxf * ozf, cz = uxf * oyf - uyf * oxf;
+        bperp = sqrtf(cx * cx + cy * cy + cz * cz);
+      }
+
+      float un_c[NC], on_c[NC], rux[NC], ruy[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];
+      float gup[NC][NSPEC];
+      ff wm_c[NC], cw_c[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        un_c[c] = on_c[c] = 0.f;
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) gup[c][s] = 0.f;
+        if (!((MASK >> c) & 1u)) continue;
+        const KCompF32& C = P.comp[c];
+        const int type = L::type(c);
+        const ff hs = hs_r[L::range(c)], md = mid_r[L::range(c)];
+        const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
+                 dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+        const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+        const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
+        const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+        un_c[c] = un.hi + un.lo;
+        on_c[c] = on.hi + on.lo;
+        // upstream gradient of this pixel, times (stop - start)/2: per component, or the total's
+        const float hsf = hs.hi + hs.lo;
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s)
+          gup[c][s] = (float)(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) *
+                      hsf;
+        wm_c[c] = cw_c[c] = ff{0.f, 0.f};
+        rux[c] = ruy[c] = rox[c] = roy[c] = eqx[c] = eqy[c] = 0.f;
+        if (type == ZL_RING || type == ZL_FEATURE) {
+          const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
+          const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+          wm_c[c] = ff_add(md, beta);
+          cw_c[c] = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+        }
+        if (type == ZL_FEATURE) {
+          const float ex = (float)(O.ex - (double)C.ox), ey = (float)(O.ey - (double)C.oy);
+          const float phi = atan2f(ey, ex) + C.c[6];
+          float sp, cp;
+          sincosf(phi, &sp, &cp);
+          const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+          rux[c] = cp * uxf + sp * uyf;
+          ruy[c] = cp * uyf - sp * uxf;
+          rox[c] = cp * ocx + sp * ocy;
+          roy[c] = cp * ocy - sp * ocx;
+          const float e2 = ex * ex + ey * ey;
+          eqx[c] = ey / e2;   // d atan2(E - X_0)/d x_0
+          eqy[c] = -ex / e2;  // d atan2(E - X_0)/d y_0
+        }
+      }
+
+      // Offset and orientation derivatives: with X - X_0 = R_los u + (X_obs - X_0) they are
+      // combinations of four per-node sums per component, completed after the node loop.
+      float fthx[NC], fthy[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) fthx[c] = fthy[c] = 0.f;
+      float wq = 0.f;  // sum over a range's components of w n E_T (the T_0 / delta derivatives)
+
+      // ---- quadrature nodes ------------------------------------------------
+#pragma unroll 1
+      for (int k = 0; k < P.n_nodes; ++k) {
+        const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
+        const float wk = P.gl_w[k];
+        float Rl = 0.f, X0 = 0.f, X1 = 0.f, X2 = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
+        float Tn = 0.f, T = 0.f, flux = 0.f, theta = 0.f;
+        float Bv[NSPEC], dB[NSPEC], sf[NSPEC], base[NSPEC], eC3[NSPEC];
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) Bv[s] = dB[s] = sf[s] = base[s] = eC3[s] = 0.f;
+        float t4s[NC], y4s[NC];  // a band's 1 - e^-y and y d ln(1 - e^-y)/dy, reused by equal bands
+#pragma unroll
+        for (int c = 0; c < NC; ++c) t4s[c] = y4s[c] = 0.f;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          if (!((MASK >> c) & 1u)) continue;
+          const KCompF32& C = P.comp[c];
+          const int type = L::type(c);
+          if (L::first(c)) {
+            Rl = node_position(hs_r[L::range(c)], xk, mid_r[L::range(c)]);
+            X0 = fmaf(Rl, uxf, oxf);
+            X1 = fmaf(Rl, uyf, oyf);
+            X2 = fmaf(Rl, uzf, ozf);
+            R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
+            rinv = rsqrt_ftz(R2);
+            if (type == ZL_CLOUD || type == ZL_BAND) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
+            R = R2 * rinv;
+            lg2R = lg2_ftz(R);
+            Tn = ex2_ftz(P.neg_delta * lg2R);
+            T = P.T0 * Tn;
+#pragma unroll
+            for (int s = 0; s < NSPEC; ++s) {
+              const float2 bd = bb_lookup_d(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
+              Bv[s] = bd.x;
+              dB[s] = bd.y;
+            }
+            if (SCAT) {
+              theta = atan2f(bperp, -(Rl + beta_h.hi));
+              flux = rinv * rinv;
+#pragma unroll
+              for (int s = 0; s < NSPEC; ++s) {
+                const KSpecF32& S = P.spec[s];
+                eC3[s] = ex2_ftz(S.C3l2e * theta);
+                base[s] = S.C1 + S.C2 * theta + eC3[s];
+                sf[s] = S.S * flux * (S.N * base[s]);
+              }
+            }
+          }
+          // component frame: X - X_0, its norm, height above the symmetry plane
+          const float Xc0 = X0 - C.ox, Xc1 = X1 - C.oy, Xc2 = X2 - C.oz;
+          float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R;
+          if (Fl::offset(C, c)) {
+            Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
+            rcinv = rsqrt_ftz(Rc2);
+            if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
+            Rc = Rc2 * rcinv;
+            lg2Rc = 0.5f * lg2_ftz(Rc2);
+          }
+          const float Z = fmaf(Rl, un_c[c], on_c[c]);
+          const float aZ = fabsf(Z);
+          const float* q = A.q[c];
+          // density = n_0 du; GR = d ln n / d R_c, GZ = d ln n / d Z; p6.. = d ln n / d (own params)
+          float du, GR, GZ, p6 = 0.f, p7 = 0.f, p8 = 0.f, p9 = 0.f, p10 = 0.f, dthx = 0.f, dthy = 0.f;
+          if (type == ZL_CLOUD) {
+            // q: alpha, beta, gamma, mu, 1/mu
+            const float zeta = aZ * rcinv;
+            const bool in = zeta < q[3];
+            const float g = in ? zeta * zeta * C.c[5] : zeta - C.c[6];
+            const float lgg = lg2_ftz(g);
+            const float gg = ex2_ftz(q[2] * lgg);
+            du = ex2_ftz(-q[0] * lg2Rc - C.c[2] * gg);
+            const float bgg = q[1] * q[2] * gg;
+            const float rg = __fdividef(1.f, g);  // g > 0 wherever it is used below
+            const float Az = zeta > 0.f ? bgg * (in ? __fdividef(2.f, zeta) : rg) : 0.f;
+            GR = (-q[0] + Az * zeta) * rcinv;
+            GZ = -copysignf(Az, Z) * rcinv;
+            p6 = -lg2Rc * kLn2;
+            p7 = -gg;
+            p8 = g > 0.f ? -q[1] * gg * lgg * kLn2 : 0.f;
+            p9 = in ? bgg * q[4] : (g > 0.f ? 0.5f * bgg * rg : 0.f);
+          } else if (type == ZL_BAND) {
+            // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
+            const float x = aZ * rcinv * C.c[1];
+            const float x2 = x * x, x6 = x2 * x2 * x2;
+            const float t2 = ex2_ftz(-kLog2e * x6);
+            const float lgx = lg2_ftz(x);
+            const float xp = Fl::p4(C, c) ? x2 * x2 : ex2_ftz(q[2] * lgx);
+            const float xpv = xp * C.c[2];
+            const float t3 = 1.f + xpv;
+            float t4 = 0.f, Y4 = 0.f;
+            bool shared = false;
+            if (Fl::runtime) {
+#pragma unroll
+              for (int j = 0; j < NC; ++j)
+                if (j < c && C.share_t4 == j && ((MASK >> j) & 1u)) {
+                  t4 = t4s[j];
+                  Y4 = y4s[j];
+                  shared = true;
+                }
+            } else if (Fl::share_first(c) && ((MASK >> L::first_band(c)) & 1u)) {
+              t4 = t4s[L::first_band(c)];
+              Y4 = y4s[L::first_band(c)];
+              shared = true;
+            }
+            if (!shared) {
+              const float qq = Rc2 * C.c[4];
+              const float qq2 = qq * qq, qq4 = qq2 * qq2, qq8 = qq4 * qq4;
+              const float y = qq8 * qq2;
+              const float emy = ex2_ftz(-kLog2e * y);
+              t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
+                             : 1.f - emy;
+              Y4 = t4 > 0.f ? y * emy * __fdividef(1.f, t4) : 1.f;  // y d ln(1 - e^-y) / d y
+            }
+            t4s[c] = t4;
+            y4s[c] = Y4;
+            du = 3.f * rcinv * t2 * t3 * t4;
+            const float it3 = __fdividef(1.f, t3);
+            const float Sx = -6.f * x6 + q[2] * xpv * it3;  // x d ln n / d x
+            GR = (-1.f - Sx + 20.f * Y4) * rcinv;
+            GZ = aZ > 0.f ? __fdividef(Sx, Z) : 0.f;  // Sx sign(Z) / |Z|
+            p6 = -Sx * q[4];
+            p7 = -xpv * it3 * C.c[2];
+            p8 = x > 0.f ? xpv * lgx * kLn2 * it3 : 0.f;
+            p9 = Y4 * q[5];
+          } else {
+            // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
+            float dR = Rc - q[0];
+            const float D2 = sq_plus_ff(lin_ff2(hs_r[L::range(c)], xk, wm_c[c]), cw_c[c]);
+            dR = dR + (D2 - dR * (Rc + q[0])) * (0.5f * rcinv);
+            float arg = dR * dR * q[1] + aZ * q[2];
+            GR = -2.f * dR * q[1];
+            GZ = Z != 0.f ? -copysignf(q[2], Z) : 0.f;
+            p6 = 2.f * dR * q[1];  // d/d R
+            p7 = dR * dR * q[3];   // d/d sigma_r = 2 dR^2 / sigma_r^3
+            p8 = aZ * q[4];        // d/d sigma_z = |Z| / sigma_z^2
+            if (type == ZL_FEATURE) {
+              const float dth = atan2f(fmaf(Rl, ruy[c], roy[c]), fmaf(Rl, rux[c], rox[c]));
+              arg = fmaf(dth * dth, q[5], arg);
+              const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
+              p9 = -gth * kDeg;                     // dtheta/dtheta_deg = -pi/180
+              p10 = dth * dth * q[6];               // 2 dth^2 / sigma_theta^3 per degree
+              const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
+              dthx = gth * (Xc1 * rr - eqx[c]);
+              dthy = gth * (-Xc0 * rr - eqy[c]);
+            }
+            du = ex2_ftz(-kLog2e * arg);
+          }
+          // emission per spectral set and its upstream-weighted sums
+          float E = 0.f, Q = 0.f;
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) {
+            const KSpecF32& S = P.spec[s];
+            const float ev = SCAT ? fmaf(S.alb[c], sf[s], S.em1[c] * Bv[s]) : S.em1[c] * Bv[s];
+            E = fmaf(gup[c][s], ev, E);
+            Q = fmaf(gup[c][s] * S.em1[c], dB[s], Q);
+          }
+          const float wdu = wk * du;        // w * density / n_0
+          const float wd = wdu * A.n0[c];  // w * density; the upstream gradient is in E and Q
+          const float coef = wd * E;
+          const int o = G::off(c);
+          const float gRr = GR * rcinv;
+          const float cG = coef * gRr, cZ = coef * GZ;
+          acc[o + 0] = fmaf(cG, Rl, acc[o + 0]);  // sum coef g_R R_los
+          acc[o + 1] += cG;                       // sum coef g_R
+          acc[o + 2] += cZ;                       // sum coef g_Z
+          acc[o + 3] = fmaf(cZ, Rl, acc[o + 3]);  // sum coef g_Z R_los
+          if (type == ZL_FEATURE) {
+            fthx[c] = fmaf(coef, dthx, fthx[c]);
+            fthy[c] = fmaf(coef, dthy, fthy[c]);
+          }
+          acc[o + 5] = fmaf(wdu, E, acc[o + 5]);
+          acc[o + 6] += coef * p6;
+          acc[o + 7] += coef * p7;
+          acc[o + 8] += coef * p8;
+          if (type != ZL_RING) acc[o + 9] += coef * p9;
+          if (type == ZL_FEATURE) acc[o + 10] += coef * p10;
+          wq = fmaf(wd, Q, wq);
+          if (last_of_range<LAYOUT, MASK>(c)) {
+            acc[G::T0] = fmaf(wq, Tn, acc[G::T0]);
+            acc[G::DELTA] = fmaf(-wq * T, lg2R * kLn2, acc[G::DELTA]);
+            wq = 0.f;
+          }
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) {
+            const KSpecF32& S = P.spec[s];
+            const float wg = wd * gup[c][s];
+            acc[G::eps(c, s)] += wg * A.one_m_alb[s][c] * Bv[s];
+            acc[G::alb(c, s)] += wg * ((SCAT ? sf[s] : 0.f) - A.eps[s][c] * Bv[s]);
+            if (SCAT) {
+              const float af = wg * S.alb[c] * flux;
+              acc[G::C(3, s)] += af * S.N * base[s];
+              const float as = af * S.S;
+              acc[G::C(0, s)] += as * (S.N + base[s] * A.dN[s][0]);
+              acc[G::C(1, s)] += as * (S.N * theta + base[s] * A.dN[s][1]);
+              acc[G::C(2, s)] += as * (S.N * theta * eC3[s] + base[s] * A.dN[s][2]);
+            }
+          }
+        }
+      }
+
+      // d/dx_0..z_0 = -sum coef g_R (X - X_0)/R - n sum coef g_Z (+ the feature's longitude term);
+      // d/di, d/dOmega = sum coef g_Z (X - X_0) . dn
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (!((MASK >> c) & 1u)) continue;
+        const KCompF32& C = P.comp[c];
+        const int o = G::off(c);
+        const float s1 = acc[o + 0], s2 = acc[o + 1], s3 = acc[o + 2], s4 = acc[o + 3];
+        const float dxc = oxf - C.ox, dyc = oyf - C.oy, dzc = ozf - C.oz;
+        acc[o + 0] = -fmaf(uxf, s1, dxc * s2) - C.nx * s3 + fthx[c];
+        acc[o + 1] = -fmaf(uyf, s1, dyc * s2) - C.ny * s3 + fthy[c];
+        acc[o + 2] = -fmaf(uzf, s1, dzc * s2) - C.nz * s3;
+        const float ui = uxf * A.dni[c][0] + uyf * A.dni[c][1] + uzf * A.dni[c][2];
+        const float di = dxc * A.dni[c][0] + dyc * A.dni[c][1] + dzc * A.dni[c][2];
+        const float uO = uxf * A.dnO[c][0] + uyf * A.dnO[c][1];
+        const float dO = dxc * A.dnO[c][0] + dyc * A.dnO[c][1];
+        acc[o + 3] = fmaf(ui, s4, di * s3);
+        acc[o + 4] = fmaf(uO, s4, dO * s3);
+      }
+    }
+
+    // ---- tile reduction: fixed shuffle tree, then warps in order ------------
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NG; ++j) {
+      float v = acc[j];
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+      if (lane == 0) red_sm[warp][j] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < NG; j += blockDim.x) {
+      double s = 0.0;
+#pragma unroll
+      for (int w = 0; w < kTile / 32; ++w) s += (double)red_sm[w][j];
+      partials[tile * NG + j] = s;
+    }
+    __syncthreads();
+  }
+}
+
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, uint32_t FLAGS>
+static void launch_one(bool scat, const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
+                       const ObsArgs& obs, const double* g_comps, const double* g_total,
+                       double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
+  if (scat)
+    bwd_f32_kernel<LAYOUT, MASK, NSPEC, true, FLAGS>
+        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles);
+  else
+    bwd_f32_kernel<LAYOUT, MASK, NSPEC, false, FLAGS>
+        <<<(unsigned)grid, kTile, 0, st>>>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles);
+}
+
+template <uint32_t LAYOUT, int NSPEC, uint32_t FLAGS>
+static cudaError_t launch_groups(const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
+                                 const ObsArgs& obs, const double* g_comps, const double* g_total,
+                                 double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
+  const bool scat = P.has_scat != 0;
+  launch_one<LAYOUT, 0x0Fu, NSPEC, FLAGS>(scat, P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+  if constexpr (LAYOUT == kLayoutDirbe) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    constexpr int NG = GradLay<LAYOUT, NSPEC>::NG;
+    launch_one<LAYOUT, 0x30u, NSPEC, FLAGS>(scat, P, A, u, n, obs, g_comps, g_total,
+                                     partials + (size_t)n_tiles * NG, n_tiles, st, grid);
+  }
+  return cudaGetLastError();
+}
+
+template <uint32_t LAYOUT, uint32_t FLAGS>
+static cudaError_t launch_bwd_nspec(const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
+                                    const ObsArgs& obs, const double* g_comps, const double* g_total,
+                                    double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
+  switch (P.n_spec) {
+    case 1: return launch_groups<LAYOUT, 1, FLAGS>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+    case 2: return launch_groups<LAYOUT, 2, FLAGS>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+    case 3: return launch_groups<LAYOUT, 3, FLAGS>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+    default: return launch_groups<LAYOUT, 4, FLAGS>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+  }
+}
+
+// The backward reads every flag but scattering (that is its SCAT parameter).
+constexpr uint32_t kBwdFlagsMask = ~2u;
+
+cudaError_t launch_bwd_f32_dirbe(const KParamsF32& P, const KGradAux& A, uint32_t flags, const double* u, int64_t n,
+                                 const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
+                                 int64_t n_tiles, cudaStream_t st, int64_t grid);
+cudaError_t launch_bwd_f32_planck(const KParamsF32& P, const KGradAux& A, uint32_t flags, const double* u, int64_t n,
+                                  const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
+                                  int64_t n_tiles, cudaStream_t st, int64_t grid);
+
+}  // namespace zl

@@ -38,6 +38,36 @@ struct Lay {
   }
 };
 
+// Compile-time properties of a model for the built-in layouts (FLAGS); bit 0 set = read them
+// from the parameter block at run time instead (any model, the generic layout):
+//   bit 1        some component scatters sunlight (albedo != 0)
+//   bit 8 + c    component c is offset from the Sun
+//   bit 16 + c   band c has p == 4 (its (zeta/dzeta)^p is a square of a square)
+//   bit 24 + c   band c reuses the first band's 1 - e^-(R/delta_r)^20 (equal delta_r and offset)
+constexpr uint32_t kFlagsRuntime = 1u;
+
+template <uint32_t F>
+struct KFlags {
+  static constexpr bool runtime = (F & 1u) != 0;
+  __device__ static __forceinline__ bool scat(const KParamsF32& P) {
+    return runtime ? P.has_scat != 0 : ((F >> 1) & 1u) != 0;
+  }
+  __device__ static __forceinline__ bool offset(const KCompF32& C, int c) {
+    return runtime ? C.zero_offset == 0 : ((F >> (8 + c)) & 1u) != 0;
+  }
+  __device__ static __forceinline__ bool p4(const KCompF32& C, int c) {
+    return runtime ? C.c[5] != 0.f : ((F >> (16 + c)) & 1u) != 0;
+  }
+  __device__ static __forceinline__ bool share_first(int c) { return ((F >> (24 + c)) & 1u) != 0; }
+};
+
+// The flag set of the built-in Kelsall models (cloud offset, bands with p = 4, band 3 reusing
+// band 1's inner-cutoff term) for the DIRBE and Planck layouts.
+constexpr uint32_t kFlagsKelsall = (1u << 8) | (7u << 17) | (1u << 27);
+
+// Flag set of a model for a layout (1 = DIRBE, 2 = Planck), or kFlagsRuntime (zl_fwd_f32.cu).
+uint32_t f32_flags(const KParamsF32& P, int layout);
+
 // Root of |obs + s u| = cutoff (line_of_sight.py:80-85) in float-float; b omits
 // z_obs u_z like the reference.  At b == 0 the root is taken with sign(+0).
 __device__ __forceinline__ ff sphere_distance_ff(ff b, ff r2, ff cut2) {

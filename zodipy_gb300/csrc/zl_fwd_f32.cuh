@@ -32,29 +32,6 @@
 
 namespace zl {
 
-// Compile-time properties of a model for the built-in layouts (FLAGS); bit 0 set = read them
-// from the parameter block at run time instead (any model, the generic layout):
-//   bit 1        some component scatters sunlight (albedo != 0)
-//   bit 8 + c    component c is offset from the Sun
-//   bit 16 + c   band c has p == 4 (its (zeta/dzeta)^p is a square of a square)
-//   bit 24 + c   band c reuses the first band's 1 - e^-(R/delta_r)^20 (equal delta_r and offset)
-constexpr uint32_t kFlagsRuntime = 1u;
-
-template <uint32_t F>
-struct KFlags {
-  static constexpr bool runtime = (F & 1u) != 0;
-  __device__ static __forceinline__ bool scat(const KParamsF32& P) {
-    return runtime ? P.has_scat != 0 : ((F >> 1) & 1u) != 0;
-  }
-  __device__ static __forceinline__ bool offset(const KCompF32& C, int c) {
-    return runtime ? C.zero_offset == 0 : ((F >> (8 + c)) & 1u) != 0;
-  }
-  __device__ static __forceinline__ bool p4(const KCompF32& C, int c) {
-    return runtime ? C.c[5] != 0.f : ((F >> (16 + c)) & 1u) != 0;
-  }
-  __device__ static __forceinline__ bool share_first(int c) { return ((F >> (24 + c)) & 1u) != 0; }
-};
-
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
 __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                       const double* __restrict__ u, int64_t n_pix,
@@ -337,10 +314,6 @@ static cudaError_t launch_f32_flags(const KParamsF32& P, const double* u, int64_
     default: return launch_f32_t<4, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
   }
 }
-
-// The flag set of the built-in Kelsall models (cloud offset, bands with p = 4, band 3 reusing
-// band 1's inner-cutoff term) for the DIRBE and Planck layouts.
-constexpr uint32_t kFlagsKelsall = (1u << 8) | (7u << 17) | (1u << 27);
 
 // Per-layout launchers (zl_fwd_f32_dirbe.cu, zl_fwd_f32_planck.cu, zl_fwd_f32_generic.cu).
 cudaError_t launch_fwd_f32_dirbe(const KParamsF32& P, uint32_t flags, bool plain_geometry, const double* u, int64_t n,
