@@ -260,8 +260,9 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             const float gg = ex2_ftz(q[2] * lgg);
             du = ex2_ftz(-q[0] * lg2Rc - C.c[2] * gg);
             const float bgg = q[1] * q[2] * gg;
-            const float rg = __fdividef(1.f, g);  // g > 0 wherever it is used below
-            const float Az = zeta > 0.f ? bgg * (in ? __fdividef(2.f, zeta) : rg) : 0.f;
+            // one reciprocal: 2 / zeta inside the widening (in), 1 / g outside (g > 0 where used)
+            const float rg = __fdividef(1.f, in ? 0.5f * zeta : g);
+            const float Az = zeta > 0.f ? bgg * rg : 0.f;
             GR = (-q[0] + Az * zeta) * rcinv;
             GZ = -copysignf(Az, Z) * rcinv;
             p6 = -lg2Rc * kLn2;
@@ -373,10 +374,11 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) {
             const KSpecF32& S = P.spec[s];
-            const float wg = wd * gup[c][s];
-            acc[G::eps(c, s)] += wg * A.one_m_alb[s][c] * Bv[s];
-            acc[G::alb(c, s)] += wg * ((SCAT ? sf[s] : 0.f) - A.eps[s][c] * Bv[s]);
+            // per node only sum w n B and w n S_flux; the pixel's constant factors follow the loop
+            acc[G::eps(c, s)] = fmaf(wd, Bv[s], acc[G::eps(c, s)]);
+            if (SCAT) acc[G::alb(c, s)] = fmaf(wd, sf[s], acc[G::alb(c, s)]);
             if (SCAT) {
+              const float wg = wd * gup[c][s];
               const float af = wg * S.alb[c] * flux;
               acc[G::C(3, s)] += af * S.N * base[s];
               const float as = af * S.S;
@@ -389,12 +391,19 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       }
 
       // d/dx_0..z_0 = -sum coef g_R (X - X_0)/R - n sum coef g_Z (+ the feature's longitude term);
-      // d/di, d/dOmega = sum coef g_Z (X - X_0) . dn
+      // d/di, d/dOmega = sum coef g_Z (X - X_0) . dn;
+      // d/d eps = g (1 - A) sum w n B,  d/d A = g (sum w n S_flux - eps sum w n B)
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         if (!((MASK >> c) & 1u)) continue;
         const KCompF32& C = P.comp[c];
         const int o = G::off(c);
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) {
+          const float sB = acc[G::eps(c, s)], sS = SCAT ? acc[G::alb(c, s)] : 0.f;
+          acc[G::eps(c, s)] = gup[c][s] * A.one_m_alb[s][c] * sB;
+          acc[G::alb(c, s)] = gup[c][s] * fmaf(-A.eps[s][c], sB, sS);
+        }
         const float s1 = acc[o + 0], s2 = acc[o + 1], s3 = acc[o + 2], s4 = acc[o + 3];
         const float dxc = oxf - C.ox, dyc = oyf - C.oy, dzc = ozf - C.oz;
         acc[o + 0] = -fmaf(uxf, s1, dxc * s2) - C.nx * s3 + fthx[c];
