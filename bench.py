@@ -505,8 +505,13 @@ def main():
 
     xu_peak = probe(0)
     fma_peak = probe(1)
+    # algorithmic work per line of sight (formula level, zodipy_gb300/roofline.py) and the pipe
+    # whose roofline rate is lower bounds the kernel
     xu_per_los = roofline.xu_ops_per_los(zl)
+    fp_per_los = roofline.fp32_ops_per_los(zl)
     xu_achieved = xu_per_los * n / (ms32 * 1e-3)
+    fp_achieved = fp_per_los * n / (ms32 * 1e-3)
+    xu_bound = xu_peak / xu_per_los <= fma_peak / fp_per_los
 
     # ---- end to end through the public API from pinned host memory ----------
     u_pinned = torch.from_numpy(u_np).pin_memory()
@@ -563,14 +568,21 @@ def main():
             "n_params": int(grad.numel()),
             "batched": batched,
             "roofline": {
-                "bound": "xu",
-                "achieved": xu_achieved / 1e9,
-                "peak": xu_peak / 1e9,
-                "unit": "Gop/s (MUFU)",
-                "frac": xu_achieved / xu_peak,
+                "bound": "xu" if xu_bound else "fp32",
+                "achieved": (xu_achieved if xu_bound else fp_achieved) / 1e9,
+                "peak": (xu_peak if xu_bound else fma_peak) / 1e9,
+                "unit": "Gop/s (MUFU)" if xu_bound else "Gop/s (FP32 FMA pipe)",
+                "frac": xu_achieved / xu_peak if xu_bound else fp_achieved / fma_peak,
                 "traffic": None,
-                "peak_source": "measured: ex2.approx probe kernel (zl_diag_pipe_probe) on this GPU in this run",
+                "peak_source": "measured in this run on this GPU: ex2.approx and fma.rn.f32 probe kernels "
+                "(zl_diag_pipe_probe); the path uses neither HBM bandwidth nor tensor cores",
+                "work": "formula-level operations per line of sight (zodipy_gb300/roofline.py): "
+                f"{xu_per_los} XU, {fp_per_los} FP32",
                 "xu_ops_per_los": xu_per_los,
+                "fp32_ops_per_los": fp_per_los,
+                "xu_frac": xu_achieved / xu_peak,
+                "fp32_frac": fp_achieved / fma_peak,
+                "implemented_xu_ops_per_los": roofline.implemented_xu_ops_per_node(zl) * zl.n_nodes,
                 "fma_peak_gops": fma_peak / 1e9,
                 "hbm_gbs_achieved": roofline.io_bytes_per_los(zl, True, True) * n / (ms32 * 1e-3) / 1e9,
                 "hbm_gbs_peak": peaks.get("hbm_gbs"),

@@ -284,8 +284,15 @@ ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t b
  * of every thread. */
 ZL_API int zl_debug_plain_geometry(int32_t on);
 
+/* Diagnostics: 1 keeps the one-pixel float32 kernel for the built-in layouts
+ * where zl_forward otherwise integrates two pixels per thread with packed
+ * float32 instructions (the Planck layout); -1 selects the two-pixel kernel
+ * for the DIRBE layout as well; 0 restores the default.  For comparing the
+ * kernels; applies to later calls of every thread. */
+ZL_API int zl_debug_one_pixel(int32_t on);
+
 /* Diagnostics: launch a pipe-throughput probe on `stream` (which = 0: MUFU
- * ex2, which = 1: FP32 FMA), `iters` iterations of 8 independent chains per
+ * ex2, which = 1: FP32 FMA, which = 2: packed FP32 FMA counted per FMA), `iters` iterations of 8 independent chains per
  * thread; *ops_per_launch receives the number of probe instructions.  The
  * caller times the launch.  sink_dev must hold >= 8 * SM-count floats. */
 ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int32_t sink_len,

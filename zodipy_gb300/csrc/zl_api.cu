@@ -14,7 +14,8 @@
 namespace zl {
 cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
                            double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
-cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
+extern int g_two_pixel_dirbe;
+cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, bool one_pixel, const double* u, int64_t n,
                            const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb,
                            int bps, int num_sms);
 int grad_count_layout(int layout, int n_spec);
@@ -347,13 +348,18 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
     const ZlSpectrum& S = m.spec[s];
     KSpecF32& K = P->spec[s];
     for (int c = 0; c < m.n_comps; ++c) {
+      const double c0 = (double)P->comp[c].c[0];  // density prefactor (n_0, 3 n_0, A, amp ...)
       if (m.family == ZL_RRM) {  // brightness.py:83: B(T) n calibration
         K.em1[c] = (float)S.calibration;
         K.alb[c] = 0.f;
+        K.outer[c] = (float)(c0 * S.calibration);
+        K.outer_alb[c] = 0.f;
         continue;
       }
       K.em1[c] = (float)((1.0 - S.albedo[c]) * S.emissivity[c]);
       K.alb[c] = (float)S.albedo[c];
+      K.outer[c] = (float)(c0 * ((1.0 - S.albedo[c]) * S.emissivity[c]));
+      K.outer_alb[c] = (float)(c0 * S.albedo[c]);
       if (S.albedo[c] != 0.0) P->has_scat = 1;
     }
     const double t1 = 2 * M_PI, t2 = 2 * S.C1, t3 = M_PI * S.C2, t4 = (std::exp(S.C3 * M_PI) + 1) / (S.C3 * S.C3 + 1);
@@ -376,6 +382,15 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
 static int g_plain_geometry = 0;
 extern "C" ZL_API int zl_debug_plain_geometry(int32_t on) {
   g_plain_geometry = on ? 1 : 0;
+  return ZL_OK;
+}
+
+// Testing hook: 1 keeps the one-pixel float32 kernel where the two-pixel (packed
+// f32x2) kernel would run, so the two can be compared.  Not part of the ABI.
+static int g_one_pixel = 0;
+extern "C" ZL_API int zl_debug_one_pixel(int32_t on) {
+  g_one_pixel = on > 0 ? 1 : 0;
+  zl::g_two_pixel_dirbe = on < 0 ? 1 : 0;  // -1: two-pixel kernel for the DIRBE layout too
   return ZL_OK;
 }
 
@@ -406,8 +421,8 @@ int forward_impl(const ZlModel* model, const double* u, int64_t n_pix, const Obs
     static thread_local KParamsF32 P;
     build_f32(*model, &P);
     const int bps = cfg.bps ? cfg.bps : 8;
-    e = launch_fwd_f32(P, detect_layout(*model), g_plain_geometry != 0, u, n_pix, OA, out_comps, out_total, st,
-                       cfg.tpb, bps, nsm);
+    e = launch_fwd_f32(P, detect_layout(*model), g_plain_geometry != 0, g_one_pixel != 0, u, n_pix, OA, out_comps,
+                       out_total, st, cfg.tpb, bps, nsm);
   }
   if (e != cudaSuccess) return cuda_fail(e, "zl_forward launch");
   return ZL_OK;

@@ -75,6 +75,9 @@ struct KCompF32 {
 
 struct KSpecF32 {
   float em1[ZL_MAX_COMPS];  // (1 - albedo) * emissivity
+  // forward: the component's density prefactor times em1 (times the albedo): the node loop sums
+  // the prefactor-free density and these constants scale each block sum once
+  float outer[ZL_MAX_COMPS], outer_alb[ZL_MAX_COMPS];
   float alb[ZL_MAX_COMPS];  // albedo
   float C1, C2, C3l2e, S, N;  // phase function (C3 pre-multiplied by log2 e), solar flux, normalisation
   float pad[3];

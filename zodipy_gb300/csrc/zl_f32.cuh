@@ -83,7 +83,7 @@ __device__ __forceinline__ ff sphere_distance_ff(ff b, ff r2, ff cut2) {
 __device__ __forceinline__ float bb_lookup(const float4* __restrict__ tab, float T, float t_min, float t_max,
                                            float inv_dt, int nT) {
   const float Tc = fminf(fmaxf(T, t_min), t_max);
-  int j = __float2int_rd((Tc - t_min) * inv_dt);
+  int j = __float2int_rd(fmaf(Tc, inv_dt, -t_min * inv_dt));  // segment index; the offset is loop-invariant
   j = min(j, nT - 2);
   const float4 e = tab[j];  // (T_j, B_j, slope_j, -)
   return fmaf(e.z, Tc - e.x, e.y);
@@ -100,6 +100,10 @@ __device__ __forceinline__ float2 bb_lookup_d(const float4* __restrict__ tab, fl
   const float slope = (T > t_min && T < t_max) ? e.z : 0.f;
   return make_float2(fmaf(e.z, Tc - e.x, e.y), slope);
 }
+
+// Quadrature nodes summed in plain float32 before each compensated addition: the
+// relative error of a block sum stays below (kSumBlock - 1) 2^-24 (positive terms).
+constexpr int kSumBlock = 8;
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float t) {
   const float y = t - c;
@@ -143,7 +147,8 @@ __device__ __forceinline__ ff sq_plus_ff2(ff w, ff c) {
 // a < b for normalised float-float values
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 
-// Fan, comet, narrow and broad band of the RRM model (number_density.py:184-342) in float32.
+// Fan, comet, narrow and broad band of the RRM model (number_density.py:184-342) in float32,
+// without the amplitude C.c[0] (the caller applies it).
 // The radial mask R_inner <= |X - X_0| <= R_outer and the narrow band's cut |beta| < beta_nb are
 // decided on float-float squares (|X - X_0|^2 = w^2 + b^2, Z^2 < sin^2(beta_nb) R^2), so float32
 // rounding cannot move a node across them; the values inside are plain float32.
@@ -160,17 +165,17 @@ __device__ __forceinline__ float rrm_masked_density(const KCompF32& C, int type,
     const float eps = za < 1.f ? 2.f - za : 1.f;
     float f = ex2_ftz(C.c[3] * sinf(ex2_ftz(eps * lg2_ftz(fabsf(beta)))));  // exp(-P sin(|beta|^eps))
     if (type == ZL_FAN && C.c[2] != 0.f) f *= ex2_ftz(C.c[2] * lg2_ftz(fmaxf(1.f - s * s, 0.f)));  // cos^Q
-    return C.c[0] * ex2_ftz(C.c[1] * lg2R) * f;
+    return ex2_ftz(C.c[1] * lg2R) * f;
   }
   const float bdeg = beta * 57.29577951308232f;
   const float radial = ex2_ftz(fmaf(C.c[1], lg2R, C.c[5]));  // (R / R_outer)^-gamma
   if (type == ZL_NARROW_BAND) {
     const ff Zf = lin_ff2(z1, x, z0);
     if (!ff_lt(ff_mul(Zf, Zf), ff_mul(ff{C.c[6], C.c[7]}, R2))) return 0.f;
-    return C.c[0] * radial * ex2_ftz(C.c[2] * (fabsf(bdeg) - C.c[3]));
+    return radial * ex2_ftz(C.c[2] * (fabsf(bdeg) - C.c[3]));
   }
   const float a = (bdeg - C.c[2]) * C.c[3], b = (bdeg + C.c[2]) * C.c[3];
-  return C.c[0] * radial * (ex2_ftz(-0.5f * kLog2e * (a * a)) + ex2_ftz(-0.5f * kLog2e * (b * b)));
+  return radial * (ex2_ftz(-0.5f * kLog2e * (a * a)) + ex2_ftz(-0.5f * kLog2e * (b * b)));
 }
 
 }  // namespace zl

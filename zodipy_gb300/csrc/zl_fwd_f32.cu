@@ -1,7 +1,7 @@
 // Float32 forward pass: choice of the compiled kernel for a model (the kernel itself is in
 // zl_fwd_f32.cuh; its instantiations are spread over one translation unit per layout so that
 // they compile in parallel).
-#include "zl_fwd_f32.cuh"
+#include "zl_fwd_f32x2.cuh"
 
 namespace zl {
 
@@ -24,12 +24,25 @@ uint32_t f32_flags(const KParamsF32& P, int layout) {
   return f;
 }
 
+int g_two_pixel_dirbe = 0;
+
 // layout: 1 = DIRBE-like, 2 = Planck-like, 0 = generic; plain_geometry selects the
-// all-float32 variant of the DIRBE layout (kept for the precision/speed study).
-cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, const double* u, int64_t n,
-                           const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+// all-float32 variant of the DIRBE layout (kept for the precision/speed study); one_pixel
+// keeps the one-pixel kernel where the two-pixel one (zl_fwd_f32x2.cuh) would run.
+cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, bool one_pixel, const double* u,
+                           int64_t n, const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
                            int num_sms) {
   const uint32_t flags = f32_flags(P, layout);
+  // The two-pixel kernel wins where its doubled per-pixel state still leaves enough warps:
+  // measured on GB300 at nside 512, Planck layout 0.79 vs 0.91 ms; for the DIRBE layout it
+  // needs 168 registers and loses (2.01 vs 1.88 ms), so that layout keeps the one-pixel
+  // kernel unless asked (two_pixel_dirbe, a testing hook).
+  if (!one_pixel && !plain_geometry && flags != kFlagsRuntime) {
+    cudaError_t e = cudaErrorNotSupported;
+    if (layout == 1 && g_two_pixel_dirbe) e = launch_fwd_f32x2_dirbe(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    if (layout == 2) e = launch_fwd_f32x2_planck(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    if (e != cudaErrorNotSupported) return e;
+  }
   if (layout == 1) return launch_fwd_f32_dirbe(P, flags, plain_geometry, u, n, obs, oc, ot, st, tpb, bps, num_sms);
   if (layout == 2) return launch_fwd_f32_planck(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
   return launch_fwd_f32_generic(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);

@@ -32,6 +32,145 @@
 
 namespace zl {
 
+// Per-pixel constants of the node loop: intersections of the line of sight with the
+// cutoff spheres, node-position and plane-height coefficients, impact parameters and the
+// feature's rotated frame (float-float where the node loop needs more than 24 bits).
+template <int NC>
+struct PixSetupF32 {
+  ff hs[NC], mh[NC], z1[NC], z0[NC], wm[NC], cw[NC];
+  // ring/feature: w -/+ w0 offsets and residual of R^2 - R0^2 = (w - w0)(w + w0) + rr
+  ff wa[NC], wb[NC];
+  float rr[NC];
+  float b2[NC], fx1[NC], fx0[NC], fy1[NC], fy0[NC];
+  float b2h, bperp;
+};
+
+template <uint32_t LAYOUT, uint32_t FLAGS, bool PRECISE, int NC>
+__device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
+                                            const ObsArgs& OA, int64_t i, PixSetupF32<NC>& S) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
+  const int nc = L::generic ? P.n_comps : NC;
+  const int nr = P.n_ranges;
+  const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+  const PixObs O = pixel_observer(OA, i, n_pix);
+  const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
+  const uint32_t outside = O.outside;
+  const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
+  const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
+
+  const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+  const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+  const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));  // u . X_obs
+
+  ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
+#pragma unroll
+  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+    if (r < nr) {
+      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
+                                                : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
+      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
+                                                    : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
+      hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+      mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+    } else {
+      hs_r[r] = ff{0.f, 0.f};
+      mid_r[r] = ff{0.f, 0.f};
+    }
+  }
+
+  // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
+  const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
+  const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
+  // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
+  S.b2h = b2h;
+  S.bperp = Fl::scat(P) ? sqrtf(b2h) : 0.f;
+
+  // per-component set-up
+  ff* hs_c = S.hs;
+  ff* mh_c = S.mh;
+  ff* z1_c = S.z1;
+  ff* z0_c = S.z0;
+  ff* wm_c = S.wm;
+  ff* cw_c = S.cw;
+  float* b2_c = S.b2;
+  float* fx1 = S.fx1;
+  float* fx0 = S.fx0;
+  float* fy1 = S.fy1;
+  float* fy0 = S.fy0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    if (c >= nc) break;
+    const KCompF32& C = P.comp[c];
+    const int type = L::generic ? C.type : L::type(c);
+    ff hs = {0.f, 0.f}, md = {0.f, 0.f};
+    if (!L::generic) {
+      hs = hs_r[L::range(c)];
+      md = mid_r[L::range(c)];
+    } else {
+#pragma unroll
+      for (int r = 0; r < ZL_MAX_RANGES; ++r)
+        if (r == C.range) {
+          hs = hs_r[r];
+          md = mid_r[r];
+        }
+    }
+    hs_c[c] = hs;
+    mh_c[c] = ff_add(md, beta_h);  // R_los + u . X_obs = hs x + mh
+    const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
+             dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+    // height above the symmetry plane, linear in the node abscissa x:
+    //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
+    const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+    const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
+    const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+    z1_c[c] = ff_mul(hs, un);
+    z0_c[c] = ff_add(ff_mul(md, un), on);
+    // |X - X_0|^2 = w^2 + b^2,  w = hs x + (mid + beta),  beta = u . (X_obs - X_0),
+    // b^2 = |X_obs - X_0|^2 - beta^2;  the ring/feature use w^2 + c' with c' = b^2 - R0^2
+    wm_c[c] = mh_c[c];
+    b2_c[c] = b2h;
+    cw_c[c] = ff{0.f, 0.f};
+    S.wa[c] = S.wb[c] = ff{0.f, 0.f};
+    S.rr[c] = 0.f;
+    if (Fl::offset(C, c) || (PRECISE && ringlike(type)) || masked(type)) {
+      const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
+      const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+      const ff bb = ff_add(d2, ff_neg(ff_mul(beta, beta)));
+      wm_c[c] = ff_add(md, beta);
+      b2_c[c] = fmaxf(bb.hi + bb.lo, 0.f);
+      cw_c[c] = masked(type) ? bb : ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
+      if (ringlike(type)) {
+        // R^2 - R0^2 = w^2 + c' = (w - w0)(w + w0) + (w0^2 + c'),  w0 = sqrt(max(-c', 0)):
+        // each factor is linear in the node abscissa and evaluated to ~1 ulp near its zero
+        const ff w0 = cw_c[c].hi < 0.f ? ff_sqrt(ff_neg(cw_c[c])) : ff{0.f, 0.f};
+        S.wa[c] = ff_add(wm_c[c], ff_neg(w0));
+        S.wb[c] = ff_add(wm_c[c], w0);
+        const ff res = ff_add(ff_mul(w0, w0), cw_c[c]);
+        S.rr[c] = res.hi + res.lo;
+      }
+    }
+    fx1[c] = fx0[c] = fy1[c] = fy0[c] = 0.f;
+    if (featurelike(type)) {
+      // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
+      // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
+      // two coordinates that are linear in the node abscissa
+      const float phi = atan2f((float)(O.ey - (double)C.oy), (float)(O.ex - (double)C.ox)) + C.c[6];
+      float sp, cp;
+      sincosf(phi, &sp, &cp);
+      const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+      const float rux = cp * uxf + sp * uyf, ruy = cp * uyf - sp * uxf;
+      const float rox = cp * ocx + sp * ocy, roy = cp * ocy - sp * ocx;
+      const float h = hs.hi + hs.lo, m = md.hi + md.lo;
+      fx1[c] = h * rux;
+      fx0[c] = fmaf(m, rux, rox);
+      fy1[c] = h * ruy;
+      fy0[c] = fmaf(m, ruy, roy);
+    }
+  }
+
+}
+
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
 __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                       const double* __restrict__ u, int64_t n_pix,
@@ -50,111 +189,28 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
     // ---- per-pixel set-up -------------------------------------------------
-    const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
-    const PixObs O = pixel_observer(OA, i, n_pix);
-    const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
-    const uint32_t outside = O.outside;
-    const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
-    const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
+    PixSetupF32<NC> PS;
+    pixel_setup<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, OA, i, PS);
+    const ff* hs_c = PS.hs;
+    const ff* mh_c = PS.mh;
+    const ff* z1_c = PS.z1;
+    const ff* z0_c = PS.z0;
+    const ff* wm_c = PS.wm;
+    const ff* cw_c = PS.cw;
+    const float* b2_c = PS.b2;
+    const float* fx1 = PS.fx1;
+    const float* fx0 = PS.fx0;
+    const float* fy1 = PS.fy1;
+    const float* fy0 = PS.fy0;
+    const float b2h = PS.b2h, bperp = PS.bperp;
 
-    const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
-    const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
-    const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));  // u . X_obs
-
-    ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
-#pragma unroll
-    for (int r = 0; r < ZL_MAX_RANGES; ++r) {
-      if (r < nr) {
-        const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
-                                                  : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
-        const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
-                                                      : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
-        hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
-        mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
-      } else {
-        hs_r[r] = ff{0.f, 0.f};
-        mid_r[r] = ff{0.f, 0.f};
-      }
-    }
-
-    // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
-    const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
-    const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
-    // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
-    const float bperp = Fl::scat(P) ? sqrtf(b2h) : 0.f;
-
-    // per-component set-up
-    ff hs_c[NC], mid_c[NC], z1_c[NC], z0_c[NC], wm_c[NC], cw_c[NC], mh_c[NC];
-    float b2_c[NC], fx1[NC], fx0[NC], fy1[NC], fy0[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      if (c >= nc) break;
-      const KCompF32& C = P.comp[c];
-      const int type = L::generic ? C.type : L::type(c);
-      ff hs = {0.f, 0.f}, md = {0.f, 0.f};
-      if (!L::generic) {
-        hs = hs_r[L::range(c)];
-        md = mid_r[L::range(c)];
-      } else {
-#pragma unroll
-        for (int r = 0; r < ZL_MAX_RANGES; ++r)
-          if (r == C.range) {
-            hs = hs_r[r];
-            md = mid_r[r];
-          }
-      }
-      hs_c[c] = hs;
-      mid_c[c] = md;
-      mh_c[c] = ff_add(md, beta_h);  // R_los + u . X_obs = hs x + mh
-      const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
-               dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
-      // height above the symmetry plane, linear in the node abscissa x:
-      //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
-      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
-      const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
-      const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
-      z1_c[c] = ff_mul(hs, un);
-      z0_c[c] = ff_add(ff_mul(md, un), on);
-      // |X - X_0|^2 = w^2 + b^2,  w = hs x + (mid + beta),  beta = u . (X_obs - X_0),
-      // b^2 = |X_obs - X_0|^2 - beta^2;  the ring/feature use w^2 + c' with c' = b^2 - R0^2
-      wm_c[c] = mh_c[c];
-      b2_c[c] = b2h;
-      cw_c[c] = ff{0.f, 0.f};
-      if (Fl::offset(C, c) || (PRECISE && ringlike(type)) || masked(type)) {
-        const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
-        const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-        const ff bb = ff_add(d2, ff_neg(ff_mul(beta, beta)));
-        wm_c[c] = ff_add(md, beta);
-        b2_c[c] = fmaxf(bb.hi + bb.lo, 0.f);
-        cw_c[c] = masked(type) ? bb : ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
-      }
-      fx1[c] = fx0[c] = fy1[c] = fy0[c] = 0.f;
-      if (featurelike(type)) {
-        // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
-        // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
-        // two coordinates that are linear in the node abscissa
-        const float phi = atan2f((float)(O.ey - (double)C.oy), (float)(O.ex - (double)C.ox)) + C.c[6];
-        float sp, cp;
-        sincosf(phi, &sp, &cp);
-        const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
-        const float rux = cp * uxf + sp * uyf, ruy = cp * uyf - sp * uxf;
-        const float rox = cp * ocx + sp * ocy, roy = cp * ocy - sp * ocx;
-        const float h = hs.hi + hs.lo, m = md.hi + md.lo;
-        fx1[c] = h * rux;
-        fx0[c] = fmaf(m, rux, rox);
-        fy1[c] = h * ruy;
-        fy0[c] = fmaf(m, ruy, roy);
-      }
-    }
-
-    float acc_s[NC][NSPEC], acc_c[NC][NSPEC];
+    // quadrature sums: plain float32 over blocks of kSumBlock nodes, Kahan-compensated across blocks
+    // (the density prefactor and emissivity / albedo multiply each block sum: S.outer, S.outer_alb)
+    float acc_s[NC][NSPEC], acc_c[NC][NSPEC], part[NC][NSPEC], partS[NC][NSPEC];
 #pragma unroll
     for (int c = 0; c < NC; ++c)
 #pragma unroll
-      for (int s = 0; s < NSPEC; ++s) {
-        acc_s[c][s] = 0.f;
-        acc_c[c][s] = 0.f;
-      }
+      for (int s = 0; s < NSPEC; ++s) acc_s[c][s] = acc_c[c][s] = part[c][s] = partS[c][s] = 0.f;
 
     // ---- quadrature nodes ------------------------------------------------
 #pragma unroll 1
@@ -162,12 +218,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
       const float wk = P.gl_w[k];
       float wh = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
-      float B[NSPEC], sf[NSPEC], t4s[NC];
+      float wB[NSPEC], wS[NSPEC], t4s[NC];  // w_k B(T) and w_k x the scattering term of the range
 #pragma unroll
-      for (int s = 0; s < NSPEC; ++s) {
-        B[s] = 0.f;
-        sf[s] = 0.f;
-      }
+      for (int s = 0; s < NSPEC; ++s) wB[s] = wS[s] = 0.f;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         t4s[c] = 0.f;
@@ -188,14 +241,14 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           lg2R = lg2_ftz(R);
           const float T = (L::generic ? C.T0 : P.T0) * ex2_ftz((L::generic ? C.neg_delta : P.neg_delta) * lg2R);  // blackbody.py:16-30
 #pragma unroll
-          for (int s = 0; s < NSPEC; ++s) B[s] = bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
+          for (int s = 0; s < NSPEC; ++s) wB[s] = wk * bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
           if (Fl::scat(P)) {  // scattering.py:11-59
             const float theta = atan2f(bperp, -wh);
             const float flux = rinv * rinv;
 #pragma unroll
             for (int s = 0; s < NSPEC; ++s) {
               const KSpecF32& S = P.spec[s];
-              sf[s] = S.S * flux * (S.N * (S.C1 + S.C2 * theta + ex2_ftz(S.C3l2e * theta)));
+              wS[s] = wk * (S.S * flux * (S.N * (S.C1 + S.C2 * theta + ex2_ftz(S.C3l2e * theta))));
             }
           }
         }
@@ -215,7 +268,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           const float zeta = fabsf(Z) * rcinv;
           const float g = zeta < C.c[4] ? zeta * zeta * C.c[5] : zeta - C.c[6];
           const float gg = ex2_ftz(C.c[3] * lg2_ftz(g));
-          dens = C.c[0] * ex2_ftz(-C.c[1] * lg2Rc - C.c[2] * gg);
+          dens = ex2_ftz(-C.c[1] * lg2Rc - C.c[2] * gg);
         } else if (type == ZL_BAND) {  // number_density.py:99-110
           const float zz = fabsf(Z) * rcinv * C.c[1];
           const float z2 = zz * zz;
@@ -244,12 +297,12 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
                            : 1.0f - ex2_ftz(-kLog2e * y);
           }
           t4s[c] = t4;
-          dens = C.c[0] * rcinv * t2 * t3 * t4;
+          dens = rcinv * t2 * t3 * t4;
         } else if (ringlike(type)) {  // ring (number_density.py:136-139) and feature (:167-181), RRM: x A
           float dR = Rc - C.c[1];
           if (precise) {
             // R^2 - R0^2 = w^2 + c' to ~1 ulp; one Newton step on R
-            const float D2 = sq_plus_ff(lin_ff2(hs_c[c], xk, wm_c[c]), cw_c[c]);
+            const float D2 = fmaf(lin_ff(hs_c[c], xk, PS.wa[c]), lin_ff(hs_c[c], xk, PS.wb[c]), PS.rr[c]);
             dR = dR + (D2 - dR * (Rc + C.c[1])) * (0.5f * rcinv);
           }
           float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
@@ -257,19 +310,30 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
             const float dth = atan2f(fmaf(fy1[c], xk.hi, fy0[c]), fmaf(fx1[c], xk.hi, fx0[c]));
             arg = fmaf(dth * dth, C.c[7], arg);
           }
-          dens = C.c[0] * ex2_ftz(-arg);
+          dens = ex2_ftz(-arg);
         } else if (type == ZL_INTERSTELLAR) {  // number_density.py:259-264
-          dens = C.c[0];
+          dens = 1.f;
         } else {
           dens = rrm_masked_density(C, type, hs_c[c], xk, wm_c[c], cw_c[c], z1_c[c], z0_c[c], Z, rcinv, lg2Rc);
         }
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
           const KSpecF32& S = P.spec[s];
-          float e = S.em1[c] * B[s];
-          if (Fl::scat(P)) e = fmaf(S.alb[c], sf[s], e);
-          kahan_add(acc_s[c][s], acc_c[c][s], wk * (e * dens));
+          part[c][s] = fmaf(wB[s], dens, part[c][s]);
+          if (Fl::scat(P)) partS[c][s] = fmaf(wS[s], dens, partS[c][s]);
         }
+      }
+      if ((k % kSumBlock) == kSumBlock - 1 || k == P.n_nodes - 1) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) {
+            const KSpecF32& S = P.spec[s];
+            const float blk = Fl::scat(P) ? fmaf(part[c][s], S.outer[c], partS[c][s] * S.outer_alb[c])
+                                          : part[c][s] * S.outer[c];
+            kahan_add(acc_s[c][s], acc_c[c][s], blk);
+            part[c][s] = partS[c][s] = 0.f;
+          }
       }
     }
 

@@ -1,0 +1,309 @@
+// Two-pixel forward kernel on Blackwell's packed FP32 instructions.
+//
+// The float32 forward kernel is bound by instruction issue, and most of what it
+// issues goes to the FMA pipes.  sm_100-class GPUs execute fma/mul/add on a pair
+// of float32 values as one instruction (fma.rn.f32x2 and friends), so a thread
+// that integrates two pixels at once -- lanes .x and .y of every float2 below --
+// issues one packed instruction where the one-pixel kernel issues two.  MUFU
+// operations (ex2, lg2, rsqrt), the blackbody table lookup, comparisons and the
+// feature's atan2 have no packed form and run per lane.
+//
+// Every lane performs exactly the one-pixel kernel's arithmetic (zl_fwd_f32.cuh):
+// the per-pixel set-up is the same function, run once per lane, and each packed
+// operation rounds as its scalar counterpart.  Subtractions a - b are written as
+// fma(b, -1, a), which rounds like a - b.
+//
+// Lanes: thread item t integrates pixels t and t + ceil(n/2), so loads and stores
+// of the [3][n] and [.][n] arrays stay coalesced for any n; for odd n the last item's
+// second lane repeats the first pixel and is not stored.
+#pragma once
+
+#include "zl_fwd_f32.cuh"
+
+namespace zl {
+
+struct ff2 {
+  float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.f), a); }  // a - b
+__device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ float2 ex2_2(float2 a) { return make_float2(ex2_ftz(a.x), ex2_ftz(a.y)); }
+__device__ __forceinline__ float2 lg2_2(float2 a) { return make_float2(lg2_ftz(a.x), lg2_ftz(a.y)); }
+__device__ __forceinline__ float2 rsqrt_2(float2 a) { return make_float2(rsqrt_ftz(a.x), rsqrt_ftz(a.y)); }
+__device__ __forceinline__ ff2 pack_ff(ff a, ff b) { return {make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+
+// lin_ff per lane: a x + b with x the node abscissa shared by both lanes
+__device__ __forceinline__ float2 lin_ff_x2(const ff2& a, ff x, const ff2& b) {
+  const float2 r = fma2(a.hi, bc2(x.hi), b.hi);
+  return add2(r, fma2(a.hi, bc2(x.lo), fma2(a.lo, bc2(x.hi), b.lo)));
+}
+
+__device__ __forceinline__ ff2 two_sum2(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  return {s, add2(sub2(a, sub2(s, bb)), sub2(b, bb))};
+}
+
+__device__ __forceinline__ ff2 quick2(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  return {s, sub2(b, sub2(s, a))};
+}
+
+// lin_ff2 per lane (float-float result)
+__device__ __forceinline__ ff2 lin_ff2_x2(const ff2& a, ff x, const ff2& b) {
+  const float2 p = mul2(a.hi, bc2(x.hi));
+  const float2 pe = fma2(a.hi, bc2(x.hi), mul2(p, bc2(-1.f)));
+  const ff2 s = two_sum2(p, b.hi);
+  return quick2(s.hi, add2(s.lo, add2(pe, fma2(a.hi, bc2(x.lo), fma2(a.lo, bc2(x.hi), b.lo)))));
+}
+
+// sq_plus_ff per lane
+__device__ __forceinline__ float2 sq_plus_ff_x2(const ff2& w, const ff2& c) {
+  return add2(fma2(w.hi, w.hi, c.hi), fma2(mul2(bc2(2.f), w.hi), w.lo, c.lo));
+}
+
+__device__ __forceinline__ void kahan_add2(float2& s, float2& c, float2 t) {
+  const float2 y = sub2(t, c);
+  const float2 s1 = add2(s, y);
+  c = sub2(sub2(s1, s), y);
+  s = s1;
+}
+
+template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS>
+__global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ KParamsF32 P,
+                                                        const double* __restrict__ u, int64_t n_pix,
+                                                        const ObsArgs OA, double* __restrict__ out_comps,
+                                                        double* __restrict__ out_total) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<FLAGS>;
+  static_assert(LAYOUT != kLayoutGeneric && !Fl::runtime, "the two-pixel kernel serves the built-in layouts");
+  constexpr int NC = L::ncomp();
+  extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
+  const int nT = P.n_temps;
+  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  __syncthreads();
+
+  const int64_t half = (n_pix + 1) / 2;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < half; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ia = t;
+    const int64_t ib = t + half < n_pix ? t + half : t;
+
+    // ---- per-pixel set-up, one lane at a time, then packed ---------------
+    ff2 hs[NC], mh[NC], z1[NC], z0[NC], wm[NC], wa[NC], wb[NC];
+    float2 b2[NC], rr[NC], fx1[NC], fx0[NC], fy1[NC], fy0[NC];
+    float2 b2h, bperp;
+    {
+      PixSetupF32<NC> A, B;
+      pixel_setup<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ia, A);
+      pixel_setup<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ib, B);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        hs[c] = pack_ff(A.hs[c], B.hs[c]);
+        mh[c] = pack_ff(A.mh[c], B.mh[c]);
+        z1[c] = pack_ff(A.z1[c], B.z1[c]);
+        z0[c] = pack_ff(A.z0[c], B.z0[c]);
+        wm[c] = pack_ff(A.wm[c], B.wm[c]);
+        wa[c] = pack_ff(A.wa[c], B.wa[c]);
+        wb[c] = pack_ff(A.wb[c], B.wb[c]);
+        b2[c] = make_float2(A.b2[c], B.b2[c]);
+        rr[c] = make_float2(A.rr[c], B.rr[c]);
+        fx1[c] = make_float2(A.fx1[c], B.fx1[c]);
+        fx0[c] = make_float2(A.fx0[c], B.fx0[c]);
+        fy1[c] = make_float2(A.fy1[c], B.fy1[c]);
+        fy0[c] = make_float2(A.fy0[c], B.fy0[c]);
+      }
+      b2h = make_float2(A.b2h, B.b2h);
+      bperp = make_float2(A.bperp, B.bperp);
+    }
+
+    // quadrature sums: plain float32 over blocks of kSumBlock nodes, Kahan-compensated across blocks
+    // (the density prefactor and emissivity / albedo multiply each block sum: S.outer, S.outer_alb)
+    float2 acc_s[NC][NSPEC], acc_c[NC][NSPEC], part[NC][NSPEC], partS[NC][NSPEC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) acc_s[c][s] = acc_c[c][s] = part[c][s] = partS[c][s] = bc2(0.f);
+
+    // ---- quadrature nodes ------------------------------------------------
+#pragma unroll 1
+    for (int k = 0; k < P.n_nodes; ++k) {
+      const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
+      const float wk = P.gl_w[k];
+      float2 wh = bc2(0.f), R2 = bc2(1.f), rinv = bc2(1.f), R = bc2(1.f), lg2R = bc2(0.f);
+      float2 wB[NSPEC], wS[NSPEC], t4s[NC];  // w_k B(T) and w_k x the scattering term of the range
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) wB[s] = wS[s] = bc2(0.f);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        t4s[c] = bc2(0.f);
+        const KCompF32& C = P.comp[c];
+        const int type = L::type(c);
+        if (L::first(c)) {
+          // brightness.py:27-33 -- heliocentric distance of the node, R^2 = w^2 + b^2, and temperature
+          wh = lin_ff_x2(hs[c], xk, mh[c]);
+          R2 = fma2(wh, wh, b2h);
+          rinv = rsqrt_2(R2);
+          if (type == ZL_CLOUD || type == ZL_BAND)
+            rinv = mul2(rinv, fma2(mul2(bc2(-0.5f), R2), mul2(rinv, rinv), bc2(1.5f)));
+          R = mul2(R2, rinv);
+          lg2R = lg2_2(R);
+          const float2 T = mul2(bc2(P.T0), ex2_2(mul2(bc2(P.neg_delta), lg2R)));  // blackbody.py:16-30
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s)
+            wB[s] = mul2(bc2(wk), make_float2(bb_lookup(tab_sm + s * nT, T.x, P.t_min, P.t_max, P.inv_dt, nT),
+                                              bb_lookup(tab_sm + s * nT, T.y, P.t_min, P.t_max, P.inv_dt, nT)));
+          if (Fl::scat(P)) {  // scattering.py:11-59
+            const float2 theta = make_float2(atan2f(bperp.x, -wh.x), atan2f(bperp.y, -wh.y));
+            const float2 flux = mul2(rinv, rinv);
+#pragma unroll
+            for (int s = 0; s < NSPEC; ++s) {
+              const KSpecF32& S = P.spec[s];
+              const float2 ph = add2(fma2(bc2(S.C2), theta, bc2(S.C1)), ex2_2(mul2(bc2(S.C3l2e), theta)));
+              wS[s] = mul2(bc2(wk), mul2(mul2(bc2(S.S), flux), mul2(bc2(S.N), ph)));
+            }
+          }
+        }
+        // own distance when the component is offset from the Sun
+        float2 Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R;
+        if (Fl::offset(C, c)) {
+          const float2 wc = lin_ff_x2(hs[c], xk, wm[c]);
+          Rc2 = fma2(wc, wc, b2[c]);
+          rcinv = rsqrt_2(Rc2);
+          if (type == ZL_BAND) rcinv = mul2(rcinv, fma2(mul2(bc2(-0.5f), Rc2), mul2(rcinv, rcinv), bc2(1.5f)));
+          Rc = mul2(Rc2, rcinv);
+          lg2Rc = mul2(bc2(0.5f), lg2_2(Rc2));
+        }
+        const float2 Z = lin_ff_x2(z1[c], xk, z0[c]);
+        float2 dens;
+        if (type == ZL_CLOUD) {  // number_density.py:60-73
+          const float2 zeta = mul2(abs2(Z), rcinv);
+          const float2 gin = mul2(mul2(zeta, zeta), bc2(C.c[5]));
+          const float2 gout = sub2(zeta, bc2(C.c[6]));
+          const float2 g = make_float2(zeta.x < C.c[4] ? gin.x : gout.x, zeta.y < C.c[4] ? gin.y : gout.y);
+          const float2 gg = ex2_2(mul2(bc2(C.c[3]), lg2_2(g)));
+          dens = ex2_2(fma2(bc2(-C.c[1]), lg2Rc, mul2(bc2(-C.c[2]), gg)));
+        } else if (type == ZL_BAND) {  // number_density.py:99-110
+          const float2 zz = mul2(mul2(abs2(Z), rcinv), bc2(C.c[1]));
+          const float2 z2 = mul2(zz, zz);
+          const float2 t2 = ex2_2(mul2(bc2(-kLog2e), mul2(mul2(z2, z2), z2)));
+          const float2 zp = Fl::p4(C, c) ? mul2(z2, z2) : ex2_2(mul2(bc2(C.c[3]), lg2_2(zz)));
+          const float2 t3 = fma2(zp, bc2(C.c[2]), bc2(1.f));
+          float2 t4;
+          if (Fl::share_first(c)) {
+            t4 = t4s[L::first_band(c)];
+          } else {
+            const float2 q = mul2(Rc2, bc2(C.c[4]));  // (R/delta_r)^2
+            const float2 q2 = mul2(q, q), q4 = mul2(q2, q2), q8 = mul2(q4, q4);
+            const float2 y = mul2(q8, q2);  // (R/delta_r)^20
+            // 1 - e^-y: below 1/4 by its series, above from ex2
+            const float2 ny = mul2(y, bc2(-1.f));
+            float2 ser = fma2(ny, bc2(1.f / 720.f), bc2(1.f / 120.f));
+            ser = fma2(ny, ser, bc2(1.f / 24.f));
+            ser = fma2(ny, ser, bc2(1.f / 6.f));
+            ser = fma2(ny, ser, bc2(0.5f));
+            ser = mul2(y, fma2(ny, ser, bc2(1.f)));
+            const float2 alt = sub2(bc2(1.f), ex2_2(mul2(bc2(-kLog2e), y)));
+            t4 = make_float2(y.x < 0.25f ? ser.x : alt.x, y.y < 0.25f ? ser.y : alt.y);
+          }
+          t4s[c] = t4;
+          dens = mul2(mul2(mul2(rcinv, t2), t3), t4);
+        } else {  // ring (number_density.py:136-139) and feature (:167-181)
+          float2 dR = sub2(Rc, bc2(C.c[1]));
+          // R^2 - R0^2 = (w - w0)(w + w0) + rr to ~1 ulp; one Newton step on R
+          const float2 D2 = fma2(lin_ff_x2(hs[c], xk, wa[c]), lin_ff_x2(hs[c], xk, wb[c]), rr[c]);
+          const float2 nt = fma2(Rc, bc2(-1.f), bc2(-C.c[1]));  // -(R + R0)
+          dR = fma2(fma2(dR, nt, D2), mul2(bc2(0.5f), rcinv), dR);
+          float2 arg = fma2(mul2(dR, dR), bc2(C.c[2]), mul2(abs2(Z), bc2(C.c[3])));
+          if (featurelike(type)) {
+            const float2 yy = fma2(fy1[c], bc2(xk.hi), fy0[c]);
+            const float2 xx = fma2(fx1[c], bc2(xk.hi), fx0[c]);
+            const float2 dth = make_float2(atan2f(yy.x, xx.x), atan2f(yy.y, xx.y));
+            arg = fma2(mul2(dth, dth), bc2(C.c[7]), arg);
+          }
+          dens = make_float2(ex2_ftz(-arg.x), ex2_ftz(-arg.y));
+        }
+#pragma unroll
+        for (int s = 0; s < NSPEC; ++s) {
+          const KSpecF32& S = P.spec[s];
+          part[c][s] = fma2(wB[s], dens, part[c][s]);
+          if (Fl::scat(P)) partS[c][s] = fma2(wS[s], dens, partS[c][s]);
+        }
+      }
+      if ((k % kSumBlock) == kSumBlock - 1 || k == P.n_nodes - 1) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+          for (int s = 0; s < NSPEC; ++s) {
+            const KSpecF32& S = P.spec[s];
+            const float2 blk = Fl::scat(P) ? fma2(part[c][s], bc2(S.outer[c]), mul2(partS[c][s], bc2(S.outer_alb[c])))
+                                           : mul2(part[c][s], bc2(S.outer[c]));
+            kahan_add2(acc_s[c][s], acc_c[c][s], blk);
+            part[c][s] = partS[c][s] = bc2(0.f);
+          }
+      }
+    }
+
+    // ---- outputs: x (stop - start)/2, component order total ----------------
+#pragma unroll
+    for (int lane = 0; lane < 2; ++lane) {
+      if (lane == 1 && ib == ia) break;
+      const int64_t i = lane ? ib : ia;
+#pragma unroll
+      for (int s = 0; s < NSPEC; ++s) {
+        double tot = 0.0;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const float as = lane ? acc_s[c][s].y : acc_s[c][s].x;
+          const float ac = lane ? acc_c[c][s].y : acc_c[c][s].x;
+          const float hh = lane ? hs[c].hi.y : hs[c].hi.x;
+          const float hl = lane ? hs[c].lo.y : hs[c].lo.x;
+          // explicit roundings: the total must equal the sum of the stored components bit for bit
+          const double v = __dmul_rn(__dsub_rn((double)as, (double)ac), __dadd_rn((double)hh, (double)hl));
+          if (out_comps) out_comps[((int64_t)s * NC + c) * n_pix + i] = v;
+          tot = (c == 0) ? v : __dadd_rn(tot, v);
+        }
+        if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
+      }
+    }
+  }
+}
+
+template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS>
+static cudaError_t launch_f32x2_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
+                                  double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+  const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
+  const int64_t items = (n + 1) / 2;
+  const int64_t blocks_needed = (items + tpb - 1) / tpb;
+  int64_t grid = (int64_t)num_sms * bps;
+  if (grid > blocks_needed) grid = blocks_needed;
+  if (grid < 1) grid = 1;
+  fwd_f32x2_kernel<NSPEC, LAYOUT, FLAGS><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
+  return cudaGetLastError();
+}
+
+template <uint32_t LAYOUT, uint32_t FLAGS>
+static cudaError_t launch_f32x2_flags(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
+                                      double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+  switch (P.n_spec) {
+    case 1: return launch_f32x2_t<1, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 2: return launch_f32x2_t<2, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 3: return launch_f32x2_t<3, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    default: return launch_f32x2_t<4, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  }
+}
+
+// Two-pixel launchers of the built-in layouts (zl_fwd_f32x2_dirbe.cu, zl_fwd_f32x2_planck.cu);
+// they return cudaErrorNotSupported for a flag set they are not compiled for.
+cudaError_t launch_fwd_f32x2_dirbe(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
+                                   const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+                                   int num_sms);
+cudaError_t launch_fwd_f32x2_planck(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
+                                    const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+                                    int num_sms);
+
+}  // namespace zl

@@ -1,0 +1,16 @@
+// Two-pixel float32 forward kernels of the DIRBE component layout (cloud | 3 bands | ring | feature).
+#include "zl_fwd_f32x2.cuh"
+
+namespace zl {
+
+cudaError_t launch_fwd_f32x2_dirbe(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
+                                   const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
+                                   int num_sms) {
+  if (flags == kFlagsKelsall)
+    return launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  if (flags == (kFlagsKelsall | 2u))
+    return launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall | 2u>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  return cudaErrorNotSupported;
+}
+
+}  // namespace zl
