@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--large", action="store_true", help="config 5: nside 2048 x 3 observers x 3 bands, GL 100")
     p.add_argument("--large-nside", type=int, default=2048)
+    p.add_argument(
+        "--profile-case",
+        choices=["fwd", "bwd", "fwd-planck"],
+        help="only run a few launches of one kernel of the workload (a target for ncu captures); no JSON",
+    )
     return p.parse_args()
 
 
@@ -324,8 +329,39 @@ def large_run(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(args):
+    """A few launches of one kernel on the bench workload, for profiler captures."""
+    import torch
+
+    from zodipy_gb300 import engine, packing
+
+    u_np, obs, earth = workload(args.nside)
+    if args.profile_case == "fwd-planck":
+        import zodipy_gb300 as zg
+        from zodipy_gb300 import units as un
+
+        model = zg.Model(857 * un.GHz, name="planck18", precision="float32")
+    else:
+        model = build_model("float32")
+    zl = model.zl_model
+    u = torch.from_numpy(u_np).cuda()
+    tab = packing.observer_table(zl, obs, earth, [0], any_mode=False)
+    obs_dev = engine.upload_observers(tab)
+    g = torch.ones((1, u.shape[1]), dtype=torch.float64, device="cuda")
+    for _ in range(max(args.steps, 1)):
+        if args.profile_case == "bwd":
+            engine.backward(zl, u, obs_dev, 1, g_total=g)
+        else:
+            engine.forward(zl, u, obs_dev, 1, "float32")
+    torch.cuda.synchronize()
+    print(f"profile case {args.profile_case}: {args.steps} launches of {u.shape[1]} lines of sight")
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return

@@ -506,7 +506,7 @@ void build_aux(const ZlModel& m, KGradAux* A) {
     A->dni[c][2] = (float)(-C.sin_i * deg);
     A->dnO[c][0] = (float)(C.cos_Omega * C.sin_i * deg);
     A->dnO[c][1] = (float)(C.sin_Omega * C.sin_i * deg);
-    A->n0[c] = (float)C.n_0;
+    A->n0[c] = (float)(C.type == ZL_BAND ? 3.0 * C.n_0 : C.n_0);  // the density's prefactor (bands: 3 n_0)
     const double* p = C.p;
     // derivative constants, with every division done here in float64
     switch (C.type) {

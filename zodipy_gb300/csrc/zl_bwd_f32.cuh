@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
   using L = Lay<LAYOUT>;
   using G = GradLay<LAYOUT, NSPEC>;
   using Fl = KFlags<FLAGS>;
+  constexpr bool KF = NSPEC == 1 && !SCAT;  // the upstream factor K = g em1 leaves the node loop
   constexpr int NC = L::ncomp();
   constexpr int NG = G::NG;
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
@@ -134,7 +135,8 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
 
       float un_c[NC], on_c[NC], rux[NC], ruy[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];
       float gup[NC][NSPEC];
-      ff wm_c[NC], cw_c[NC];
+      ff wa_c[NC], wb_c[NC];  // ring/feature: R^2 - R0^2 = (w - w0)(w + w0) + rr_c
+      float rr_c[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         un_c[c] = on_c[c] = 0.f;
@@ -157,13 +159,19 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
         for (int s = 0; s < NSPEC; ++s)
           gup[c][s] = (float)(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) *
                       hsf;
-        wm_c[c] = cw_c[c] = ff{0.f, 0.f};
+        wa_c[c] = wb_c[c] = ff{0.f, 0.f};
+        rr_c[c] = 0.f;
         rux[c] = ruy[c] = rox[c] = roy[c] = eqx[c] = eqy[c] = 0.f;
         if (type == ZL_RING || type == ZL_FEATURE) {
           const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
           const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-          wm_c[c] = ff_add(md, beta);
-          cw_c[c] = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+          const ff wm = ff_add(md, beta);
+          const ff cw = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+          const ff w0 = cw.hi < 0.f ? ff_sqrt(ff_neg(cw)) : ff{0.f, 0.f};
+          wa_c[c] = ff_add(wm, ff_neg(w0));
+          wb_c[c] = ff_add(wm, w0);
+          const ff res = ff_add(ff_mul(w0, w0), cw);
+          rr_c[c] = res.hi + res.lo;
         }
         if (type == ZL_FEATURE) {
           const float ex = (float)(O.ex - (double)C.ox), ey = (float)(O.ey - (double)C.oy);
@@ -187,6 +195,9 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
 #pragma unroll
       for (int c = 0; c < NC; ++c) fthx[c] = fthy[c] = 0.f;
       float wq = 0.f;  // sum over a range's components of w n E_T (the T_0 / delta derivatives)
+      float kpix[NC];  // K = g em1 per component (one spectral set, no scattering)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) kpix[c] = KF ? gup[c][0] * P.spec[0].em1[c] : 0.f;
 
       // ---- quadrature nodes ------------------------------------------------
 #pragma unroll 1
@@ -304,7 +315,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             }
             t4s[c] = t4;
             y4s[c] = Y4;
-            du = 3.f * rcinv * t2 * t3 * t4;
+            du = rcinv * t2 * t3 * t4;  // the factor 3 of 3 n_0 is in A.n0 (and in d/dn_0 below)
             const float it3 = __fdividef(1.f, t3);
             const float Sx = -6.f * x6 + q[2] * xpv * it3;  // x d ln n / d x
             GR = (-1.f - Sx + 20.f * Y4) * rcinv;
@@ -316,7 +327,8 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           } else {
             // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
             float dR = Rc - q[0];
-            const float D2 = sq_plus_ff(lin_ff2(hs_r[L::range(c)], xk, wm_c[c]), cw_c[c]);
+            const ff hs = hs_r[L::range(c)];
+            const float D2 = fmaf(lin_ff(hs, xk, wa_c[c]), lin_ff(hs, xk, wb_c[c]), rr_c[c]);
             dR = dR + (D2 - dR * (Rc + q[0])) * (0.5f * rcinv);
             float arg = dR * dR * q[1] + aZ * q[2];
             GR = -2.f * dR * q[1];
@@ -337,17 +349,22 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             du = ex2_ftz(-kLog2e * arg);
           }
           // emission per spectral set and its upstream-weighted sums
+          // E = sum_s g_s e_s and Q = sum_s g_s em1_s dB_s/dT.  With one spectral set and no
+          // scattering both are K B and K dB/dT with K = g em1 constant over the pixel's nodes:
+          // then the sums below run without K and the pixel's K scales them after the loop.
           float E = 0.f, Q = 0.f;
+          if (!KF) {
 #pragma unroll
-          for (int s = 0; s < NSPEC; ++s) {
-            const KSpecF32& S = P.spec[s];
-            const float ev = SCAT ? fmaf(S.alb[c], sf[s], S.em1[c] * Bv[s]) : S.em1[c] * Bv[s];
-            E = fmaf(gup[c][s], ev, E);
-            Q = fmaf(gup[c][s] * S.em1[c], dB[s], Q);
+            for (int s = 0; s < NSPEC; ++s) {
+              const KSpecF32& S = P.spec[s];
+              const float ev = SCAT ? fmaf(S.alb[c], sf[s], S.em1[c] * Bv[s]) : S.em1[c] * Bv[s];
+              E = fmaf(gup[c][s], ev, E);
+              Q = fmaf(gup[c][s] * S.em1[c], dB[s], Q);
+            }
           }
           const float wdu = wk * du;        // w * density / n_0
           const float wd = wdu * A.n0[c];  // w * density; the upstream gradient is in E and Q
-          const float coef = wd * E;
+          const float coef = KF ? wd * Bv[0] : wd * E;
           const int o = G::off(c);
           const float gRr = GR * rcinv;
           const float cG = coef * gRr, cZ = coef * GZ;
@@ -359,14 +376,15 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
             fthx[c] = fmaf(coef, dthx, fthx[c]);
             fthy[c] = fmaf(coef, dthy, fthy[c]);
           }
-          acc[o + 5] = fmaf(wdu, E, acc[o + 5]);
+          acc[o + 5] = fmaf(wdu, KF ? Bv[0] : E, acc[o + 5]);
           acc[o + 6] += coef * p6;
           acc[o + 7] += coef * p7;
           acc[o + 8] += coef * p8;
           if (type != ZL_RING) acc[o + 9] += coef * p9;
           if (type == ZL_FEATURE) acc[o + 10] += coef * p10;
-          wq = fmaf(wd, Q, wq);
+          wq = KF ? fmaf(wd, kpix[c], wq) : fmaf(wd, Q, wq);
           if (last_of_range<LAYOUT, MASK>(c)) {
+            if (KF) wq *= dB[0];
             acc[G::T0] = fmaf(wq, Tn, acc[G::T0]);
             acc[G::DELTA] = fmaf(-wq * T, lg2R * kLn2, acc[G::DELTA]);
             wq = 0.f;
@@ -404,7 +422,16 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           acc[G::eps(c, s)] = gup[c][s] * A.one_m_alb[s][c] * sB;
           acc[G::alb(c, s)] = gup[c][s] * fmaf(-A.eps[s][c], sB, sS);
         }
-        const float s1 = acc[o + 0], s2 = acc[o + 1], s3 = acc[o + 2], s4 = acc[o + 3];
+        // with KF the coefficient sums lack the pixel factor K = g em1 (see the node loop)
+        const float kf = KF ? kpix[c] : 1.f;
+        if (KF) {
+#pragma unroll
+          for (int j = 5; j < G::npar(L::type(c)); ++j) acc[o + j] *= kf;
+          fthx[c] *= kf;
+          fthy[c] *= kf;
+        }
+        if (L::type(c) == ZL_BAND) acc[o + 5] *= 3.f;  // d/dn_0 of 3 n_0 (...)
+        const float s1 = kf * acc[o + 0], s2 = kf * acc[o + 1], s3 = kf * acc[o + 2], s4 = kf * acc[o + 3];
         const float dxc = oxf - C.ox, dyc = oyf - C.oy, dzc = ozf - C.oz;
         acc[o + 0] = -fmaf(uxf, s1, dxc * s2) - C.nx * s3 + fthx[c];
         acc[o + 1] = -fmaf(uyf, s1, dyc * s2) - C.ny * s3 + fthy[c];

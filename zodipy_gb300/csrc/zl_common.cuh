@@ -100,7 +100,7 @@ struct KGradAux {
   float dni[ZL_MAX_COMPS][3];  // d n_hat / d i   [per degree]
   float dnO[ZL_MAX_COMPS][2];  // d n_hat / d Omega [per degree] (z component is 0)
   float q[ZL_MAX_COMPS][8];    // type constants in natural units (see zl_api.cu)
-  float n0[ZL_MAX_COMPS];      // n_0 (densities are evaluated per unit n_0)
+  float n0[ZL_MAX_COMPS];      // density prefactor: n_0, or 3 n_0 for a band (densities are evaluated without it)
   float eps[ZL_MAX_SPEC][ZL_MAX_COMPS], one_m_alb[ZL_MAX_SPEC][ZL_MAX_COMPS];  // per spectral set
   float dN[ZL_MAX_SPEC][3];    // d N / d C1, C2, C3 of the phase normalisation, per spectral set
 };
