@@ -344,9 +344,9 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         if (c >= nc) break;
-        // explicit roundings: the total must equal the sum of the stored components bit for bit
-        const double v = __dmul_rn(__dsub_rn((double)acc_s[c][s], (double)acc_c[c][s]),
-                                   __dadd_rn((double)hs_c[c].hi, (double)hs_c[c].lo));
+        // the compensated sum times (stop - start)/2 in float32 (GB300's FP64 pipe is narrow);
+        // the total is the float64 sum of the stored components, so it equals their sum exactly
+        const double v = (double)((acc_s[c][s] - acc_c[c][s]) * (hs_c[c].hi + hs_c[c].lo));
         if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + i] = v;
         tot = (c == 0) ? v : __dadd_rn(tot, v);
       }

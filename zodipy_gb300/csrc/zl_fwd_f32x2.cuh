@@ -262,8 +262,8 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
           const float ac = lane ? acc_c[c][s].y : acc_c[c][s].x;
           const float hh = lane ? hs[c].hi.y : hs[c].hi.x;
           const float hl = lane ? hs[c].lo.y : hs[c].lo.x;
-          // explicit roundings: the total must equal the sum of the stored components bit for bit
-          const double v = __dmul_rn(__dsub_rn((double)as, (double)ac), __dadd_rn((double)hh, (double)hl));
+          // as the one-pixel kernel: float32 product, float64 total of the stored components
+          const double v = (double)((as - ac) * (hh + hl));
           if (out_comps) out_comps[((int64_t)s * NC + c) * n_pix + i] = v;
           tot = (c == 0) ? v : __dadd_rn(tot, v);
         }
