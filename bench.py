@@ -7,8 +7,11 @@ kernel, per-component + total outputs.  Inputs are synthetic (HEALPix centres
 computed here); no dataset is involved.
 
   value     LOS/s of the float32 kernel with inputs resident in HBM
-  e2e       LOS/s through Model.evaluate_xyz from pinned host memory (H2D of
-            the unit vectors and D2H of the total map inside the timed region)
+  e2e       LOS/s through Model.evaluate_xyz from pinned host memory (the unit
+            vectors move host -> device and the total map device -> host inside
+            the timed region; on Grace-Blackwell the kernel reads and writes the
+            mapped host buffers directly over NVLink-C2C, elsewhere the call
+            pipelines chunked copies through two copy streams)
   extras    float64 plain-kernel LOS/s, float32-vs-float64 max/median relative
             error over the full map, XU roofline fraction, CPU baseline
 
@@ -558,6 +561,15 @@ def main():
         res = model.evaluate_xyz(u_pinned, obs_np, earth, return_comps=False, precision="float32", out=out_pinned)
         return res
 
+    from zodipy_gb300 import model as model_mod
+
+    mapped = engine.mapped_pointer(u_pinned) is not None and engine.mapped_pointer(out_pinned) is not None
+    e2e_mode = (
+        "zero copy: the kernel reads the pinned unit vectors and writes the pinned result (mapped host memory)"
+        if mapped and model_mod._ZERO_COPY
+        else "chunked host-to-device / device-to-host copies pipelined with the kernels"
+    )
+
     for _ in range(max(args.warmup, 3)):
         e2e_step()
     torch.cuda.synchronize()
@@ -629,6 +641,7 @@ def main():
                 "unit": "LOS/s",
                 "h2d_bytes_per_step": int(u_np.nbytes) + 64,
                 "d2h_bytes_per_step": int(n * 8),
+                "transfer": e2e_mode,
             },
             "gpu_launches": args.steps,
             "clocks": clk,

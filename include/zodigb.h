@@ -274,6 +274,13 @@ ZL_API int zl_density_grid(const ZlModel* model, const double* x_dev, int32_t nx
                            const double* z_dev, int32_t nz, const double* earth_xyz_host, double* out_dev,
                            void* stream);
 
+/* Device address of page-locked host memory (cudaHostGetDevicePointer).  On
+ * GPUs that reach host memory over a coherent link (Grace-Blackwell NVLink-C2C)
+ * the kernels can read their inputs from and write their outputs to such
+ * memory directly: pass the returned pointers to zl_forward instead of device
+ * buffers.  Returns ZL_ERR_CUDA when the memory is not mapped. */
+ZL_API int zl_mapped_pointer(const void* host_ptr, void** dev_ptr);
+
 /* Launch configuration used by zl_forward for a precision, as chosen by the
  * autotuner (threads per block, blocks per SM; 0 = library default). */
 ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);

@@ -184,6 +184,7 @@ _SIGNATURES = {
     ),
     "zl_debug_plain_geometry": (ctypes.c_int, [ctypes.c_int32]),
     "zl_debug_one_pixel": (ctypes.c_int, [ctypes.c_int32]),
+    "zl_mapped_pointer": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "zl_diag_pipe_probe": (
         ctypes.c_int,
         [ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p],

@@ -663,3 +663,19 @@ extern "C" ZL_API int zl_density_grid(const ZlModel* model, const double* x, int
   if (e != cudaSuccess) return cuda_fail(e, "zl_density_grid launch");
   return ZL_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Host memory the device can address directly
+// ---------------------------------------------------------------------------
+extern "C" ZL_API int zl_mapped_pointer(const void* host_ptr, void** dev_ptr) {
+  if (!host_ptr || !dev_ptr) return fail(ZL_ERR_ARG, "NULL pointer argument");
+  void* d = nullptr;
+  const cudaError_t e = cudaHostGetDevicePointer(&d, const_cast<void*>(host_ptr), 0);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // not mapped: clear the error state and report
+    *dev_ptr = nullptr;
+    return fail(ZL_ERR_CUDA, "host pointer is not mapped for device access: %s", cudaGetErrorName(e));
+  }
+  *dev_ptr = d;
+  return ZL_OK;
+}

@@ -327,3 +327,30 @@ def directions(lon_dev, lat_dev, rotation=None, out=None, stream: int | None = N
     )
     _lib.check(rc, "zl_directions")
     return out
+
+
+def mapped_pointer(host_tensor) -> int | None:
+    """Device address of a page-locked CPU tensor (``zl_mapped_pointer``), or None if unmapped."""
+    if not host_tensor.is_pinned():
+        return None
+    p = ctypes.c_void_p()
+    rc = _lib.load().zl_mapped_pointer(ctypes.c_void_p(host_tensor.data_ptr()), ctypes.byref(p))
+    return p.value if rc == _lib.ZL_OK and p.value else None
+
+
+def forward_ptr(zl_model, u_ptr: int, n: int, observers_dev, n_obs: int, precision, out_comps_ptr, out_total_ptr,
+                stream: int | None = None) -> None:
+    """``zl_forward`` on raw addresses (device buffers or mapped host memory)."""
+    _torch()
+    rc = _lib.load().zl_forward(
+        ctypes.byref(zl_model),
+        ctypes.c_void_p(u_ptr),
+        int(n),
+        ctypes.c_void_p(observers_dev.data_ptr()),
+        n_obs,
+        precision_code(precision),
+        ctypes.c_void_p(out_comps_ptr or 0),
+        ctypes.c_void_p(out_total_ptr or 0),
+        ctypes.c_void_p(stream if stream is not None else current_stream_handle(observers_dev.device)),
+    )
+    _lib.check(rc, "zl_forward")

@@ -348,6 +348,12 @@ class Model:
                 u_host = torch.from_numpy(np.ascontiguousarray(np.asarray(unit_vectors, dtype=np.float64).reshape(3, n)))
             if not u_host.is_pinned():
                 u_host = u_host.pin_memory()
+            if not per_pixel and _ZERO_COPY:
+                res = _zero_copy_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out)
+                if res is not None:
+                    return res
+            if not per_pixel and n >= 2 * _PIPE_CHUNK:
+                return _pipelined_host_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out)
             u_dev = u_host.to("cuda", non_blocking=True)
         if per_pixel:
             # time-ordered input: positions per pixel, cutoff flags OR-ed over the call on the
@@ -369,6 +375,106 @@ class Model:
         host.copy_(res, non_blocking=True)
         torch.cuda.current_stream().synchronize()
         return host if out is not None else host.numpy()
+
+
+# Host arrays: where the GPU addresses page-locked host memory directly (Grace-Blackwell over
+# NVLink-C2C), the kernel reads the unit vectors from and writes the result to host memory
+# (zero copy: the data crosses the link while the kernel computes).  Otherwise calls of at
+# least two chunks of _PIPE_CHUNK pixels are pipelined through copy streams.
+_ZERO_COPY = True
+_PIPE_CHUNK = 1 << 20
+_COPY_STREAMS: dict = {}
+
+
+def _copy_streams():
+    """Two copy streams per device (host-to-device, device-to-host), created once."""
+    import torch
+
+    dev = torch.cuda.current_device()
+    if dev not in _COPY_STREAMS:
+        _COPY_STREAMS[dev] = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+    return _COPY_STREAMS[dev]
+
+
+def _result_buffer(zl, n, return_comps, all_spec, out):
+    import torch
+
+    ns, nc = zl.n_spec, zl.n_comps
+    full_shape = (ns, nc, n) if return_comps else (ns, n)
+    res_shape = full_shape if all_spec else full_shape[1:]
+    if out is None:
+        return torch.empty(res_shape, dtype=torch.float64, pin_memory=True), res_shape
+    if not isinstance(out, torch.Tensor) or tuple(out.shape) != tuple(res_shape) or out.dtype != torch.float64:
+        raise ValueError(f"out must be a float64 CPU tensor of shape {tuple(res_shape)}")
+    return out, res_shape
+
+
+def _zero_copy_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out):
+    """One launch on mapped host memory; None when either buffer is not device-addressable."""
+    import torch
+
+    host, _ = _result_buffer(zl, u_host.shape[1], return_comps, all_spec, out)
+    pu = engine.mapped_pointer(u_host)
+    po = engine.mapped_pointer(host) if host.is_contiguous() else None
+    if pu is None or po is None:
+        return None
+    engine.forward_ptr(zl, pu, u_host.shape[1], obs_dev, 1, prec, po if return_comps else None,
+                       None if return_comps else po)
+    torch.cuda.current_stream().synchronize()
+    return host if out is not None else host.numpy()
+
+
+def _pipelined_host_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out):
+    """zl_forward over host arrays in chunks: the copy of chunk i+1 in, the kernel on chunk i and
+    the copy of chunk i-1 out run concurrently (two device slots, two copy streams, the
+    caller's stream for the kernels).  Returns the host result like ``Model._evaluate``."""
+    import torch
+
+    n = u_host.shape[1]
+    ns, nc = zl.n_spec, zl.n_comps
+    rows = ns * (nc if return_comps else 1)
+    host, _ = _result_buffer(zl, n, return_comps, all_spec, out)
+    host_rows = host.view(rows, n)
+    main = torch.cuda.current_stream()
+    h2d, d2h = _copy_streams()
+    ch = _PIPE_CHUNK
+    slots = 2
+    u_buf = [torch.empty(3 * ch, dtype=torch.float64, device="cuda") for _ in range(slots)]
+    o_buf = [torch.empty(rows * ch, dtype=torch.float64, device="cuda") for _ in range(slots)]
+    ev_in = [torch.cuda.Event() for _ in range(slots)]
+    ev_run = [torch.cuda.Event() for _ in range(slots)]
+    ev_out = [torch.cuda.Event() for _ in range(slots)]
+    h2d.wait_stream(main)
+    bounds = list(range(0, n, _PIPE_CHUNK)) + [n]
+    for i in range(len(bounds) - 1):
+        k = i % slots
+        b, e = bounds[i], bounds[i + 1]
+        m = e - b
+        u_view = u_buf[k][: 3 * m].view(3, m)
+        with torch.cuda.stream(h2d):
+            if i >= slots:
+                h2d.wait_event(ev_run[k])  # the kernel of chunk i - 2 has read this slot
+            for r in range(3):
+                u_view[r].copy_(u_host[r, b:e], non_blocking=True)
+            ev_in[k].record(h2d)
+        main.wait_event(ev_in[k])
+        if i >= slots:
+            main.wait_event(ev_out[k])  # chunk i - 2's result has left this slot
+        o_view = o_buf[k][: rows * m]
+        if return_comps:
+            engine.forward(zl, u_view, obs_dev, 1, prec, True, False, out_comps=o_view.view(ns, nc, m))
+        else:
+            engine.forward(zl, u_view, obs_dev, 1, prec, False, True, out_total=o_view.view(ns, m))
+        ev_run[k].record(main)
+        with torch.cuda.stream(d2h):
+            d2h.wait_event(ev_run[k])
+            o_rows = o_view.view(rows, m)
+            for r in range(rows):
+                host_rows[r, b:e].copy_(o_rows[r], non_blocking=True)
+            ev_out[k].record(d2h)
+    main.wait_stream(d2h)
+    main.synchronize()
+    return host if out is not None else host.numpy()
 
 
 __all__ = ["Model", "Kelsall"]
