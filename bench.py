@@ -43,6 +43,12 @@ OBSTIME = "2022-01-01T00:00:00"
 CPU_SAMPLE = 1 << 18
 
 
+def workload_name(nside: int) -> str:
+    """The workload both arms report (config.workload)."""
+    return (f"DIRBE 25um, HEALPix nside {nside} ({12 * nside * nside} LOS), obspos (0.7071,0.7071,0) AU, GL 50, "
+            "6 component maps + total")
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -208,7 +214,8 @@ def reference_arm(args):
         "dtype": "f64",
         "data": "synthetic",
         "config": {
-            "workload": f"DIRBE 25um, HEALPix nside {args.nside}, obspos (0.7071,0.7071,0) AU, GL 50",
+            "workload": workload_name(args.nside),
+            "implementation": "ZodiPy's numpy path (its CPU restatement), float64, all host cores",
             "sample_los_per_step": n,
             "l2": "n/a (CPU)",
         },
@@ -601,8 +608,8 @@ def main():
             "dtype": "f32",
             "data": "synthetic",
             "config": {
-                "workload": f"DIRBE 25um, HEALPix nside {args.nside} ({n} LOS), obspos (0.7071,0.7071,0) AU, GL 50, "
-                "float32-bulk kernel, 6 component maps + total",
+                "workload": workload_name(args.nside),
+                "implementation": "libzodigb float32-bulk kernel (float-float where needed), one GPU",
                 "l2": "flushed (256 MB write) before every timed step",
                 "parallelism": f"replicas x{world}, no collective on the data path",
             },
