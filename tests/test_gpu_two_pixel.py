@@ -71,3 +71,27 @@ def test_two_pixel_time_ordered(lib):
     zl = zg.Model(25 * u_.micron).zl_model
     dirs = random_sphere(n, seed=3)
     _check(_run(zl, dirs, obs, earth, False, tod=True), _run(zl, dirs, obs, earth, True, tod=True))
+
+
+@pytest.mark.parametrize("bands", [(25.0,), (1.25,), (12.0, 25.0, 60.0)])
+def test_component_paired_equals_one_pixel(lib, bands):
+    """The DIRBE layout's default kernel pairs components in packed lanes; same tolerance."""
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import _lib
+    from zodipy_gb300 import units as u_
+    from zodipy_gb300.autograd import fuse_models
+    from zodipy_gb300.healpix import random_sphere
+
+    zl = fuse_models([zg.Model(b * u_.micron) for b in bands])
+    dirs = random_sphere(1001, seed=5)
+    obs, earth = np.array([0.75, 0.66, 0.01]), np.array([0.76, 0.65, 0.0])
+    lib_ = _lib.load()
+    _lib.check(lib_.zl_debug_one_pixel(0), "default kernel")
+    a = _run(zl, dirs, obs, earth, one_pixel=True)
+    _lib.check(lib_.zl_debug_one_pixel(0), "default kernel")
+    from zodipy_gb300 import engine, packing
+    import torch
+
+    tab = packing.observer_table(zl, obs, earth, [0], any_mode=False)
+    comps, total = engine.forward(zl, torch.from_numpy(dirs).cuda(), engine.upload_observers(tab), 1, "float32")
+    _check((comps.cpu().numpy(), total.cpu().numpy()), a)

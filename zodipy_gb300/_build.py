@@ -26,6 +26,7 @@ SOURCES = [
     "zl_fwd_f32_generic.cu",
     "zl_fwd_f32x2_dirbe.cu",
     "zl_fwd_f32x2_planck.cu",
+    "zl_fwd_dirbe_cp.cu",
     "zl_bwd_f32.cu",
     "zl_bwd_f32_dirbe.cu",
     "zl_bwd_f32_planck.cu",

@@ -1,7 +1,7 @@
 // Float32 forward pass: choice of the compiled kernel for a model (the kernel itself is in
 // zl_fwd_f32.cuh; its instantiations are spread over one translation unit per layout so that
 // they compile in parallel).
-#include "zl_fwd_f32x2.cuh"
+#include "zl_fwd_dirbe.cuh"
 
 namespace zl {
 
@@ -37,9 +37,13 @@ cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry,
   // measured on GB300 at nside 512, Planck layout 0.79 vs 0.91 ms; for the DIRBE layout it
   // needs 168 registers and loses (2.01 vs 1.88 ms), so that layout keeps the one-pixel
   // kernel unless asked (two_pixel_dirbe, a testing hook).
+  // The DIRBE layout runs the component-paired kernel (zl_fwd_dirbe.cuh): ring/feature and
+  // band 1/2 in packed lanes, one pixel per thread.
   if (!one_pixel && !plain_geometry && flags != kFlagsRuntime) {
     cudaError_t e = cudaErrorNotSupported;
-    if (layout == 1 && g_two_pixel_dirbe) e = launch_fwd_f32x2_dirbe(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    if (layout == 1)
+      e = g_two_pixel_dirbe ? launch_fwd_f32x2_dirbe(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms)
+                            : launch_fwd_dirbe_cp(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
     if (layout == 2) e = launch_fwd_f32x2_planck(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
     if (e != cudaErrorNotSupported) return e;
   }
