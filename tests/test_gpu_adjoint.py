@@ -189,3 +189,44 @@ def test_backward_rejects_small_workspace(lib):
         None, ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ws.data_ptr()), 16, None,
     )
     assert rc == _lib.ZL_ERR_SPACE and "workspace" in _lib.last_error()
+
+
+@pytest.mark.parametrize(
+    "bands,per_comp",
+    [((25.0,), False), ((1.25,), False), ((12.0, 25.0), False), ((1.25, 2.2, 3.5, 4.9), False), ((25.0,), True)],
+)
+def test_paired_adjoint_equals_scalar_kernel(lib, bands, per_comp):
+    """The DIRBE layout's component-paired adjoint kernels (ring/feature and bands 1/2
+    in packed lanes) against the scalar kernel on the same inputs: the same gradient to
+    float32 rounding of the node sums (sensitivity metric of this file, REL 1e-5)."""
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import _lib, engine, packing, params
+    from zodipy_gb300 import units as u_
+    from zodipy_gb300.autograd import fuse_models
+    from zodipy_gb300.healpix import random_sphere
+
+    models = [zg.Model(b * u_.micron) for b in bands]
+    zl = fuse_models(models)
+    dirs = torch.from_numpy(random_sphere(5003, seed=11)).cuda()
+    tab = packing.observer_table(zl, [0.75, 0.66, 0.01], [0.76, 0.65, 0.0], [0], any_mode=False)
+    obs = engine.upload_observers(tab)
+    gen = torch.Generator("cuda").manual_seed(4)
+    n = dirs.shape[1]
+    shape = (len(bands), zl.n_comps, n) if per_comp else (len(bands), n)
+    g = 0.5 + torch.rand(shape, dtype=torch.float64, device="cuda", generator=gen)
+    kw = {"g_comps": g} if per_comp else {"g_total": g}
+    try:
+        _lib.check(lib.zl_debug_one_pixel(1), "scalar kernels")
+        ref = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
+    finally:
+        _lib.check(lib.zl_debug_one_pixel(0), "default kernels")
+    got = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
+    names = params.names(zl, models[0].comp_labels)
+    theta = params.vector_from_model(zl)
+    scale = np.maximum(np.abs(theta), 1.0)
+    s_got, s_ref = got * scale, ref * scale
+    dev = np.abs(s_got - s_ref) / (np.abs(s_ref) + 1e-7 * np.abs(s_ref).max())
+    worst = int(np.argmax(dev))
+    assert dev.max() <= 1e-5, f"{names[worst]}: paired {got[worst]:.9e} scalar {ref[worst]:.9e} ({dev.max():.2e})"

@@ -29,6 +29,7 @@ SOURCES = [
     "zl_fwd_dirbe_cp.cu",
     "zl_bwd_f32.cu",
     "zl_bwd_f32_dirbe.cu",
+    "zl_bwd_dirbe_cp.cu",
     "zl_bwd_f32_planck.cu",
     "zl_diag.cu",
     "zl_static.cu",

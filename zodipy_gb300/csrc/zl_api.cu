@@ -15,6 +15,7 @@ namespace zl {
 cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
                            double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
 extern int g_two_pixel_dirbe;
+extern int g_bwd_unpaired;
 cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, bool one_pixel, const double* u, int64_t n,
                            const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb,
                            int bps, int num_sms);
@@ -385,11 +386,13 @@ extern "C" ZL_API int zl_debug_plain_geometry(int32_t on) {
   return ZL_OK;
 }
 
-// Testing hook: 1 keeps the one-pixel float32 kernel where the two-pixel (packed
-// f32x2) kernel would run, so the two can be compared.  Not part of the ABI.
+// Testing hook: 1 keeps the one-pixel, unpaired float32 kernels (forward and
+// adjoint) where the packed f32x2 kernels would run, so the two can be compared.
+// Not part of the ABI.
 static int g_one_pixel = 0;
 extern "C" ZL_API int zl_debug_one_pixel(int32_t on) {
   g_one_pixel = on > 0 ? 1 : 0;
+  zl::g_bwd_unpaired = g_one_pixel;
   zl::g_two_pixel_dirbe = on < 0 ? 1 : 0;  // -1: two-pixel kernel for the DIRBE layout too
   return ZL_OK;
 }

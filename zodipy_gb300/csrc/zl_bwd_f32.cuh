@@ -66,6 +66,445 @@ __host__ __device__ constexpr bool last_of_range(int c) {
   return true;
 }
 
+// Entries of the gradient vector a launch with component mask MASK writes: its
+// components' own parameters, T_0 and delta, its components' emissivities and
+// albedos, and with scattering the phase function and irradiance of every set.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT>
+__host__ __device__ constexpr bool grad_used(int j) {
+  using G = GradLay<LAYOUT, NSPEC>;
+  if (j == G::T0 || j == G::DELTA) return true;
+  for (int c = 0; c < Lay<LAYOUT>::ncomp(); ++c) {
+    if (!((MASK >> c) & 1u)) continue;
+    if (j >= G::off(c) && j < G::off(c) + G::npar(Lay<LAYOUT>::type(c))) return true;
+    for (int s = 0; s < NSPEC; ++s)
+      if (j == G::eps(c, s) || j == G::alb(c, s)) return true;
+  }
+  if (SCAT)
+    for (int s = 0; s < NSPEC; ++s)
+      for (int k = 0; k < 4; ++k)
+        if (j == G::C(k, s)) return true;
+  return false;
+}
+
+// Per-pixel quantities of the adjoint (constant over the quadrature nodes).
+template <int NC, int NSPEC>
+struct BwdPix {
+  ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];  // (stop - start)/2 and (stop + start)/2 per LOS range
+  ff beta_h;                                     // obs . u
+  float uxf, uyf, uzf, oxf, oyf, ozf, bperp;
+  float un_c[NC], on_c[NC];                      // u . n_c and (obs - X_0,c) . n_c
+  float rux[NC], ruy[NC], rox[NC], roy[NC];      // the feature's rotated u and obs - X_0
+  float eqx[NC], eqy[NC];                        // d atan2(E - X_0) / d x_0, d y_0
+  float gup[NC][NSPEC];                          // upstream gradient times (stop - start)/2
+  ff wa_c[NC], wb_c[NC];                         // ring/feature: R^2 - R0^2 = (w - w0)(w + w0) + rr_c
+  float rr_c[NC];
+};
+
+// Pixel set-up (as the forward kernel) for the components in MASK.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
+__device__ __forceinline__ void bwd_pixel_setup(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
+                                                const ObsArgs& OA, const double* __restrict__ g_comps,
+                                                const double* __restrict__ g_total, int64_t i,
+                                                BwdPix<Lay<LAYOUT>::ncomp(), NSPEC>& B) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<FLAGS>;
+  constexpr int NC = L::ncomp();
+  const int nr = P.n_ranges;
+  const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+  const PixObs O = pixel_observer(OA, i, n_pix);
+  const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
+  const uint32_t outside = O.outside;
+  B.uxf = ux.hi, B.uyf = uy.hi, B.uzf = uz.hi;
+  B.oxf = ox.hi, B.oyf = oy.hi, B.ozf = oz.hi;
+  const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+  const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+  B.beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));
+#pragma unroll
+  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+    bool used = false;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
+    if (used && r < nr) {
+      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
+                                                : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
+      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
+                                                    : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
+      B.hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+      B.mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+    } else {
+      B.hs_r[r] = B.mid_r[r] = ff{0.f, 0.f};
+    }
+  }
+  B.bperp = 0.f;
+  if (SCAT) {
+    const float cx = B.uyf * B.ozf - B.uzf * B.oyf, cy = B.uzf * B.oxf - B.uxf * B.ozf,
+                cz = B.uxf * B.oyf - B.uyf * B.oxf;
+    B.bperp = sqrtf(cx * cx + cy * cy + cz * cz);
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    B.un_c[c] = B.on_c[c] = 0.f;
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) B.gup[c][s] = 0.f;
+    B.wa_c[c] = B.wb_c[c] = ff{0.f, 0.f};
+    B.rr_c[c] = 0.f;
+    B.rux[c] = B.ruy[c] = B.rox[c] = B.roy[c] = B.eqx[c] = B.eqy[c] = 0.f;
+    if (!((MASK >> c) & 1u)) continue;
+    const KCompF32& C = P.comp[c];
+    const int type = L::type(c);
+    const ff hs = B.hs_r[L::range(c)], md = B.mid_r[L::range(c)];
+    const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
+             dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+    const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+    const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
+    const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+    B.un_c[c] = un.hi + un.lo;
+    B.on_c[c] = on.hi + on.lo;
+    // upstream gradient of this pixel, times (stop - start)/2: per component, or the total's
+    const float hsf = hs.hi + hs.lo;
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s)
+      B.gup[c][s] =
+          (float)(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) * hsf;
+    if (type == ZL_RING || type == ZL_FEATURE) {
+      const ff beta = !Fl::offset(C, c) ? B.beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
+      const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+      const ff wm = ff_add(md, beta);
+      const ff cw = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+      const ff w0 = cw.hi < 0.f ? ff_sqrt(ff_neg(cw)) : ff{0.f, 0.f};
+      B.wa_c[c] = ff_add(wm, ff_neg(w0));
+      B.wb_c[c] = ff_add(wm, w0);
+      const ff res = ff_add(ff_mul(w0, w0), cw);
+      B.rr_c[c] = res.hi + res.lo;
+    }
+    if (type == ZL_FEATURE) {
+      const float ex = (float)(O.ex - (double)C.ox), ey = (float)(O.ey - (double)C.oy);
+      const float phi = atan2f(ey, ex) + C.c[6];
+      float sp, cp;
+      sincosf(phi, &sp, &cp);
+      const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+      B.rux[c] = cp * B.uxf + sp * B.uyf;
+      B.ruy[c] = cp * B.uyf - sp * B.uxf;
+      B.rox[c] = cp * ocx + sp * ocy;
+      B.roy[c] = cp * ocy - sp * ocx;
+      const float e2 = ex * ex + ey * ey;
+      B.eqx[c] = ey / e2;   // d atan2(E - X_0)/d x_0
+      B.eqy[c] = -ex / e2;  // d atan2(E - X_0)/d y_0
+    }
+  }
+}
+
+// One LOS range at one quadrature node: position, distance from the Sun, grain
+// temperature, blackbody value and slope per spectral set, scattering terms.
+template <int NSPEC>
+struct NodeR {
+  float Rl, X0, X1, X2, R2, rinv, R, lg2R, Tn, T, flux, theta;
+  float Bv[NSPEC], dB[NSPEC], sf[NSPEC], base[NSPEC], eC3[NSPEC];
+};
+
+// NEWTON: one Newton step on 1/R (the cloud and the bands use R^-1 directly).
+template <int NSPEC, bool SCAT, int NC>
+__device__ __forceinline__ void node_range(const KParamsF32& P, const BwdPix<NC, NSPEC>& B, int r, bool newton, ff xk,
+                                           const float4* __restrict__ tab_sm, int nT, NodeR<NSPEC>& N) {
+  N.Rl = node_position(B.hs_r[r], xk, B.mid_r[r]);
+  N.X0 = fmaf(N.Rl, B.uxf, B.oxf);
+  N.X1 = fmaf(N.Rl, B.uyf, B.oyf);
+  N.X2 = fmaf(N.Rl, B.uzf, B.ozf);
+  N.R2 = fmaf(N.X0, N.X0, fmaf(N.X1, N.X1, N.X2 * N.X2));
+  N.rinv = rsqrt_ftz(N.R2);
+  if (newton) N.rinv = N.rinv * fmaf(-0.5f * N.R2, N.rinv * N.rinv, 1.5f);
+  N.R = N.R2 * N.rinv;
+  N.lg2R = lg2_ftz(N.R);
+  N.Tn = ex2_ftz(P.neg_delta * N.lg2R);
+  N.T = P.T0 * N.Tn;
+#pragma unroll
+  for (int s = 0; s < NSPEC; ++s) {
+    const float2 bd = bb_lookup_d(tab_sm + s * nT, N.T, P.t_min, P.t_max, P.inv_dt, nT);
+    N.Bv[s] = bd.x;
+    N.dB[s] = bd.y;
+  }
+  N.theta = N.flux = 0.f;
+#pragma unroll
+  for (int s = 0; s < NSPEC; ++s) N.sf[s] = N.base[s] = N.eC3[s] = 0.f;
+  if (SCAT) {
+    N.theta = atan2f(B.bperp, -(N.Rl + B.beta_h.hi));
+    N.flux = N.rinv * N.rinv;
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) {
+      const KSpecF32& S = P.spec[s];
+      N.eC3[s] = ex2_ftz(S.C3l2e * N.theta);
+      N.base[s] = S.C1 + S.C2 * N.theta + N.eC3[s];
+      N.sf[s] = S.S * N.flux * (S.N * N.base[s]);
+    }
+  }
+}
+
+// Density of one component at a node (without n_0) and its log-derivatives:
+// GR = d ln n / d R_c, GZ = d ln n / d Z, p6.. = d ln n / d (own parameters).
+struct CompTerms {
+  float du, GR, GZ, rcinv, p6, p7, p8, p9, p10, dthx, dthy;
+};
+
+// t4s / y4s: a band's 1 - e^-y and y d ln(1 - e^-y)/dy, reused by equal bands.
+template <uint32_t LAYOUT, uint32_t MASK, uint32_t FLAGS, int NC, int NSPEC>
+__device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, const KGradAux& A,
+                                                const BwdPix<NC, NSPEC>& B, ff xk, const NodeR<NSPEC>& N,
+                                                float* t4s, float* y4s) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<FLAGS>;
+  const KCompF32& C = P.comp[c];
+  const int type = L::type(c);
+  CompTerms t;
+  t.p6 = t.p7 = t.p8 = t.p9 = t.p10 = t.dthx = t.dthy = 0.f;
+  // component frame: X - X_0, its norm, height above the symmetry plane
+  const float Xc0 = N.X0 - C.ox, Xc1 = N.X1 - C.oy, Xc2 = N.X2 - C.oz;
+  float Rc2 = N.R2, rcinv = N.rinv, Rc = N.R, lg2Rc = N.lg2R;
+  if (Fl::offset(C, c)) {
+    Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
+    rcinv = rsqrt_ftz(Rc2);
+    if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
+    Rc = Rc2 * rcinv;
+    lg2Rc = 0.5f * lg2_ftz(Rc2);
+  }
+  t.rcinv = rcinv;
+  const float Z = fmaf(N.Rl, B.un_c[c], B.on_c[c]);
+  const float aZ = fabsf(Z);
+  const float* q = A.q[c];
+  if (type == ZL_CLOUD) {
+    // q: alpha, beta, gamma, mu, 1/mu
+    const float zeta = aZ * rcinv;
+    const bool in = zeta < q[3];
+    const float g = in ? zeta * zeta * C.c[5] : zeta - C.c[6];
+    const float lgg = lg2_ftz(g);
+    const float gg = ex2_ftz(q[2] * lgg);
+    t.du = ex2_ftz(-q[0] * lg2Rc - C.c[2] * gg);
+    const float bgg = q[1] * q[2] * gg;
+    // one reciprocal: 2 / zeta inside the widening (in), 1 / g outside (g > 0 where used)
+    const float rg = __fdividef(1.f, in ? 0.5f * zeta : g);
+    const float Az = zeta > 0.f ? bgg * rg : 0.f;
+    t.GR = (-q[0] + Az * zeta) * rcinv;
+    t.GZ = -copysignf(Az, Z) * rcinv;
+    t.p6 = -lg2Rc * kLn2;
+    t.p7 = -gg;
+    t.p8 = g > 0.f ? -q[1] * gg * lgg * kLn2 : 0.f;
+    t.p9 = in ? bgg * q[4] : (g > 0.f ? 0.5f * bgg * rg : 0.f);
+  } else if (type == ZL_BAND) {
+    // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
+    const float x = aZ * rcinv * C.c[1];
+    const float x2 = x * x, x6 = x2 * x2 * x2;
+    const float t2 = ex2_ftz(-kLog2e * x6);
+    const float lgx = lg2_ftz(x);
+    const float xp = Fl::p4(C, c) ? x2 * x2 : ex2_ftz(q[2] * lgx);
+    const float xpv = xp * C.c[2];
+    const float t3 = 1.f + xpv;
+    float t4 = 0.f, Y4 = 0.f;
+    bool shared = false;
+    if (Fl::runtime) {
+#pragma unroll
+      for (int j = 0; j < NC; ++j)
+        if (j < c && C.share_t4 == j && ((MASK >> j) & 1u)) {
+          t4 = t4s[j];
+          Y4 = y4s[j];
+          shared = true;
+        }
+    } else if (Fl::share_first(c) && ((MASK >> L::first_band(c)) & 1u)) {
+      t4 = t4s[L::first_band(c)];
+      Y4 = y4s[L::first_band(c)];
+      shared = true;
+    }
+    if (!shared) {
+      const float qq = Rc2 * C.c[4];
+      const float qq2 = qq * qq, qq4 = qq2 * qq2, qq8 = qq4 * qq4;
+      const float y = qq8 * qq2;
+      const float emy = ex2_ftz(-kLog2e * y);
+      t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
+                     : 1.f - emy;
+      Y4 = t4 > 0.f ? y * emy * __fdividef(1.f, t4) : 1.f;  // y d ln(1 - e^-y) / d y
+    }
+    t4s[c] = t4;
+    y4s[c] = Y4;
+    t.du = rcinv * t2 * t3 * t4;  // the factor 3 of 3 n_0 is in A.n0 (and in d/dn_0 below)
+    const float it3 = __fdividef(1.f, t3);
+    const float Sx = -6.f * x6 + q[2] * xpv * it3;  // x d ln n / d x
+    t.GR = (-1.f - Sx + 20.f * Y4) * rcinv;
+    t.GZ = aZ > 0.f ? __fdividef(Sx, Z) : 0.f;  // Sx sign(Z) / |Z|
+    t.p6 = -Sx * q[4];
+    t.p7 = -xpv * it3 * C.c[2];
+    t.p8 = x > 0.f ? xpv * lgx * kLn2 * it3 : 0.f;
+    t.p9 = Y4 * q[5];
+  } else {
+    // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
+    float dR = Rc - q[0];
+    const ff hs = B.hs_r[L::range(c)];
+    const float D2 = fmaf(lin_ff(hs, xk, B.wa_c[c]), lin_ff(hs, xk, B.wb_c[c]), B.rr_c[c]);
+    dR = dR + (D2 - dR * (Rc + q[0])) * (0.5f * rcinv);
+    float arg = dR * dR * q[1] + aZ * q[2];
+    t.GR = -2.f * dR * q[1];
+    t.GZ = Z != 0.f ? -copysignf(q[2], Z) : 0.f;
+    t.p6 = 2.f * dR * q[1];  // d/d R
+    t.p7 = dR * dR * q[3];   // d/d sigma_r = 2 dR^2 / sigma_r^3
+    t.p8 = aZ * q[4];        // d/d sigma_z = |Z| / sigma_z^2
+    if (type == ZL_FEATURE) {
+      const float dth = atan2f(fmaf(N.Rl, B.ruy[c], B.roy[c]), fmaf(N.Rl, B.rux[c], B.rox[c]));
+      arg = fmaf(dth * dth, q[5], arg);
+      const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
+      t.p9 = -gth * kDeg;                   // dtheta/dtheta_deg = -pi/180
+      t.p10 = dth * dth * q[6];             // 2 dth^2 / sigma_theta^3 per degree
+      const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
+      t.dthx = gth * (Xc1 * rr - B.eqx[c]);
+      t.dthy = gth * (-Xc0 * rr - B.eqy[c]);
+    }
+    t.du = ex2_ftz(-kLog2e * arg);
+  }
+  return t;
+}
+
+// Node sums of one component.  The emission per spectral set and its upstream-weighted
+// sums E = sum_s g_s e_s and Q = sum_s g_s em1_s dB_s/dT: with one spectral set and no
+// scattering (KF) both are K B and K dB/dT with K = g em1 constant over the pixel's
+// nodes; the sums then run without K and the pixel's K scales them after the loop.
+// wq: sum over a range's components of w n E_T (the T_0 / delta derivatives), flushed
+// into acc by the range's last component.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, int NC, int NG>
+__device__ __forceinline__ void comp_accumulate(int c, const KParamsF32& P, const KGradAux& A,
+                                                const BwdPix<NC, NSPEC>& B, float wk, const NodeR<NSPEC>& N,
+                                                const CompTerms& t, const float* kpix, float& wq, float* fthx,
+                                                float* fthy, float (&acc)[NG]) {
+  using L = Lay<LAYOUT>;
+  using G = GradLay<LAYOUT, NSPEC>;
+  constexpr bool KF = NSPEC == 1 && !SCAT;
+  const int type = L::type(c);
+  float E = 0.f, Q = 0.f;
+  if (!KF) {
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) {
+      const KSpecF32& S = P.spec[s];
+      const float ev = SCAT ? fmaf(S.alb[c], N.sf[s], S.em1[c] * N.Bv[s]) : S.em1[c] * N.Bv[s];
+      E = fmaf(B.gup[c][s], ev, E);
+      Q = fmaf(B.gup[c][s] * S.em1[c], N.dB[s], Q);
+    }
+  }
+  const float wdu = wk * t.du;      // w * density / n_0
+  const float wd = wdu * A.n0[c];  // w * density; the upstream gradient is in E and Q
+  const float coef = KF ? wd * N.Bv[0] : wd * E;
+  const int o = G::off(c);
+  const float gRr = t.GR * t.rcinv;
+  const float cG = coef * gRr, cZ = coef * t.GZ;
+  acc[o + 0] = fmaf(cG, N.Rl, acc[o + 0]);  // sum coef g_R R_los
+  acc[o + 1] += cG;                         // sum coef g_R
+  acc[o + 2] += cZ;                         // sum coef g_Z
+  acc[o + 3] = fmaf(cZ, N.Rl, acc[o + 3]);  // sum coef g_Z R_los
+  if (type == ZL_FEATURE) {
+    fthx[c] = fmaf(coef, t.dthx, fthx[c]);
+    fthy[c] = fmaf(coef, t.dthy, fthy[c]);
+  }
+  acc[o + 5] = fmaf(wdu, KF ? N.Bv[0] : E, acc[o + 5]);
+  acc[o + 6] += coef * t.p6;
+  acc[o + 7] += coef * t.p7;
+  acc[o + 8] += coef * t.p8;
+  if (type != ZL_RING) acc[o + 9] += coef * t.p9;
+  if (type == ZL_FEATURE) acc[o + 10] += coef * t.p10;
+  wq = KF ? fmaf(wd, kpix[c], wq) : fmaf(wd, Q, wq);
+  if (last_of_range<LAYOUT, MASK>(c)) {
+    if (KF) wq *= N.dB[0];
+    acc[G::T0] = fmaf(wq, N.Tn, acc[G::T0]);
+    acc[G::DELTA] = fmaf(-wq * N.T, N.lg2R * kLn2, acc[G::DELTA]);
+    wq = 0.f;
+  }
+#pragma unroll
+  for (int s = 0; s < NSPEC; ++s) {
+    const KSpecF32& S = P.spec[s];
+    // per node only sum w n B and w n S_flux; the pixel's constant factors follow the loop
+    acc[G::eps(c, s)] = fmaf(wd, N.Bv[s], acc[G::eps(c, s)]);
+    if (SCAT) acc[G::alb(c, s)] = fmaf(wd, N.sf[s], acc[G::alb(c, s)]);
+    if (SCAT) {
+      const float wg = wd * B.gup[c][s];
+      const float af = wg * S.alb[c] * N.flux;
+      acc[G::C(3, s)] += af * S.N * N.base[s];
+      const float as = af * S.S;
+      acc[G::C(0, s)] += as * (S.N + N.base[s] * A.dN[s][0]);
+      acc[G::C(1, s)] += as * (S.N * N.theta + N.base[s] * A.dN[s][1]);
+      acc[G::C(2, s)] += as * (S.N * N.theta * N.eC3[s] + N.base[s] * A.dN[s][2]);
+    }
+  }
+}
+
+// After the node loop: d/dx_0..z_0 = -sum coef g_R (X - X_0)/R - n sum coef g_Z (+ the
+// feature's longitude term); d/di, d/dOmega = sum coef g_Z (X - X_0) . dn;
+// d/d eps = g (1 - A) sum w n B,  d/d A = g (sum w n S_flux - eps sum w n B).
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, int NC, int NG>
+__device__ __forceinline__ void bwd_finalize(const KParamsF32& P, const KGradAux& A, const BwdPix<NC, NSPEC>& B,
+                                             const float* kpix, float* fthx, float* fthy, float (&acc)[NG]) {
+  using L = Lay<LAYOUT>;
+  using G = GradLay<LAYOUT, NSPEC>;
+  constexpr bool KF = NSPEC == 1 && !SCAT;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    if (!((MASK >> c) & 1u)) continue;
+    const KCompF32& C = P.comp[c];
+    const int o = G::off(c);
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) {
+      const float sB = acc[G::eps(c, s)], sS = SCAT ? acc[G::alb(c, s)] : 0.f;
+      acc[G::eps(c, s)] = B.gup[c][s] * A.one_m_alb[s][c] * sB;
+      acc[G::alb(c, s)] = B.gup[c][s] * fmaf(-A.eps[s][c], sB, sS);
+    }
+    // with KF the coefficient sums lack the pixel factor K = g em1 (see the node loop)
+    const float kf = KF ? kpix[c] : 1.f;
+    if (KF) {
+#pragma unroll
+      for (int j = 5; j < G::npar(L::type(c)); ++j) acc[o + j] *= kf;
+      fthx[c] *= kf;
+      fthy[c] *= kf;
+    }
+    if (L::type(c) == ZL_BAND) acc[o + 5] *= 3.f;  // d/dn_0 of 3 n_0 (...)
+    const float s1 = kf * acc[o + 0], s2 = kf * acc[o + 1], s3 = kf * acc[o + 2], s4 = kf * acc[o + 3];
+    const float dxc = B.oxf - C.ox, dyc = B.oyf - C.oy, dzc = B.ozf - C.oz;
+    acc[o + 0] = -fmaf(B.uxf, s1, dxc * s2) - C.nx * s3 + fthx[c];
+    acc[o + 1] = -fmaf(B.uyf, s1, dyc * s2) - C.ny * s3 + fthy[c];
+    acc[o + 2] = -fmaf(B.uzf, s1, dzc * s2) - C.nz * s3;
+    const float ui = B.uxf * A.dni[c][0] + B.uyf * A.dni[c][1] + B.uzf * A.dni[c][2];
+    const float di = dxc * A.dni[c][0] + dyc * A.dni[c][1] + dzc * A.dni[c][2];
+    const float uO = B.uxf * A.dnO[c][0] + B.uyf * A.dnO[c][1];
+    const float dO = dxc * A.dnO[c][0] + dyc * A.dnO[c][1];
+    acc[o + 3] = fmaf(ui, s4, di * s3);
+    acc[o + 4] = fmaf(uO, s4, dO * s3);
+  }
+}
+
+// Block start: the blackbody tables into shared memory; the reduction rows zeroed
+// (entries the launch never writes stay zero).
+template <int NSPEC, int NG>
+__device__ __forceinline__ void bwd_block_init(const KParamsF32& P, float4* tab_sm, float (*red_sm)[NG]) {
+  const int nT = P.n_temps;
+  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  for (int t = threadIdx.x; t < (kTile / 32) * NG; t += blockDim.x) red_sm[t / NG][t % NG] = 0.f;
+  __syncthreads();
+}
+
+// Tile reduction: a fixed shuffle tree per written entry, then the warps in order.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, int NG>
+__device__ __forceinline__ void bwd_tile_reduce(const float (&acc)[NG], float (*red_sm)[NG],
+                                                double* __restrict__ partials, int64_t tile) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NG; ++j) {
+    if (!grad_used<LAYOUT, MASK, NSPEC, SCAT>(j)) continue;
+    float v = acc[j];
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    if (lane == 0) red_sm[warp][j] = v;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < NG; j += blockDim.x) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < kTile / 32; ++w) s += (double)red_sm[w][j];
+    partials[tile * NG + j] = s;
+  }
+  __syncthreads();
+}
+
 // MASK selects the components this launch differentiates (bit c = component c).
 // A model's components are split into groups that each own their LOS ranges, so
 // every group launch carries only its own accumulators; parameters shared by
@@ -81,16 +520,13 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
                                                         double* __restrict__ partials, int64_t n_tiles) {
   using L = Lay<LAYOUT>;
   using G = GradLay<LAYOUT, NSPEC>;
-  using Fl = KFlags<FLAGS>;
   constexpr bool KF = NSPEC == 1 && !SCAT;  // the upstream factor K = g em1 leaves the node loop
   constexpr int NC = L::ncomp();
   constexpr int NG = G::NG;
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
+  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);
   const int nT = P.n_temps;
-  for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
-  __syncthreads();
-  const int nr = P.n_ranges;
 
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t i = tile * kTile + threadIdx.x;
@@ -99,369 +535,39 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
     for (int j = 0; j < NG; ++j) acc[j] = 0.f;
 
     if (i < n_pix) {
-      // ---- per-pixel set-up (as the forward kernel) ---------------------------
-      const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
-      const PixObs O = pixel_observer(OA, i, n_pix);
-      const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
-      const uint32_t outside = O.outside;
-      const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
-      const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
-      const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
-      const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
-      const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));
-      ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
-#pragma unroll
-      for (int r = 0; r < ZL_MAX_RANGES; ++r) {
-        bool used = false;
-#pragma unroll
-        for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
-        if (used && r < nr) {
-          const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
-                                                    : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
-          const ff sp = ((outside >> (2 * r + 1)) & 1u)
-                            ? ff{(float)kEps, 0.f}
-                            : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
-          hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
-          mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
-        } else {
-          hs_r[r] = mid_r[r] = ff{0.f, 0.f};
-        }
-      }
-      float bperp = 0.f;
-      if (SCAT) {
-        const float cx = uyf * ozf - uzf * oyf, cy = uzf * oxf - uxf * ozf, cz = uxf * oyf - uyf * oxf;
-        bperp = sqrtf(cx * cx + cy * cy + cz * cz);
-      }
-
-      float un_c[NC], on_c[NC], rux[NC], ruy[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];
-      float gup[NC][NSPEC];
-      ff wa_c[NC], wb_c[NC];  // ring/feature: R^2 - R0^2 = (w - w0)(w + w0) + rr_c
-      float rr_c[NC];
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        un_c[c] = on_c[c] = 0.f;
-#pragma unroll
-        for (int s = 0; s < NSPEC; ++s) gup[c][s] = 0.f;
-        if (!((MASK >> c) & 1u)) continue;
-        const KCompF32& C = P.comp[c];
-        const int type = L::type(c);
-        const ff hs = hs_r[L::range(c)], md = mid_r[L::range(c)];
-        const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
-                 dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
-        const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
-        const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
-        const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
-        un_c[c] = un.hi + un.lo;
-        on_c[c] = on.hi + on.lo;
-        // upstream gradient of this pixel, times (stop - start)/2: per component, or the total's
-        const float hsf = hs.hi + hs.lo;
-#pragma unroll
-        for (int s = 0; s < NSPEC; ++s)
-          gup[c][s] = (float)(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) *
-                      hsf;
-        wa_c[c] = wb_c[c] = ff{0.f, 0.f};
-        rr_c[c] = 0.f;
-        rux[c] = ruy[c] = rox[c] = roy[c] = eqx[c] = eqy[c] = 0.f;
-        if (type == ZL_RING || type == ZL_FEATURE) {
-          const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
-          const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-          const ff wm = ff_add(md, beta);
-          const ff cw = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
-          const ff w0 = cw.hi < 0.f ? ff_sqrt(ff_neg(cw)) : ff{0.f, 0.f};
-          wa_c[c] = ff_add(wm, ff_neg(w0));
-          wb_c[c] = ff_add(wm, w0);
-          const ff res = ff_add(ff_mul(w0, w0), cw);
-          rr_c[c] = res.hi + res.lo;
-        }
-        if (type == ZL_FEATURE) {
-          const float ex = (float)(O.ex - (double)C.ox), ey = (float)(O.ey - (double)C.oy);
-          const float phi = atan2f(ey, ex) + C.c[6];
-          float sp, cp;
-          sincosf(phi, &sp, &cp);
-          const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
-          rux[c] = cp * uxf + sp * uyf;
-          ruy[c] = cp * uyf - sp * uxf;
-          rox[c] = cp * ocx + sp * ocy;
-          roy[c] = cp * ocy - sp * ocx;
-          const float e2 = ex * ex + ey * ey;
-          eqx[c] = ey / e2;   // d atan2(E - X_0)/d x_0
-          eqy[c] = -ex / e2;  // d atan2(E - X_0)/d y_0
-        }
-      }
-
+      BwdPix<NC, NSPEC> B;
+      bwd_pixel_setup<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, B);
       // Offset and orientation derivatives: with X - X_0 = R_los u + (X_obs - X_0) they are
       // combinations of four per-node sums per component, completed after the node loop.
       float fthx[NC], fthy[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) fthx[c] = fthy[c] = 0.f;
-      float wq = 0.f;  // sum over a range's components of w n E_T (the T_0 / delta derivatives)
+      float wq = 0.f;
       float kpix[NC];  // K = g em1 per component (one spectral set, no scattering)
 #pragma unroll
-      for (int c = 0; c < NC; ++c) kpix[c] = KF ? gup[c][0] * P.spec[0].em1[c] : 0.f;
+      for (int c = 0; c < NC; ++c) kpix[c] = KF ? B.gup[c][0] * P.spec[0].em1[c] : 0.f;
 
-      // ---- quadrature nodes ------------------------------------------------
 #pragma unroll 1
       for (int k = 0; k < P.n_nodes; ++k) {
         const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
         const float wk = P.gl_w[k];
-        float Rl = 0.f, X0 = 0.f, X1 = 0.f, X2 = 0.f, R2 = 1.f, rinv = 1.f, R = 1.f, lg2R = 0.f;
-        float Tn = 0.f, T = 0.f, flux = 0.f, theta = 0.f;
-        float Bv[NSPEC], dB[NSPEC], sf[NSPEC], base[NSPEC], eC3[NSPEC];
-#pragma unroll
-        for (int s = 0; s < NSPEC; ++s) Bv[s] = dB[s] = sf[s] = base[s] = eC3[s] = 0.f;
-        float t4s[NC], y4s[NC];  // a band's 1 - e^-y and y d ln(1 - e^-y)/dy, reused by equal bands
+        NodeR<NSPEC> N;
+        float t4s[NC], y4s[NC];
 #pragma unroll
         for (int c = 0; c < NC; ++c) t4s[c] = y4s[c] = 0.f;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           if (!((MASK >> c) & 1u)) continue;
-          const KCompF32& C = P.comp[c];
           const int type = L::type(c);
-          if (L::first(c)) {
-            Rl = node_position(hs_r[L::range(c)], xk, mid_r[L::range(c)]);
-            X0 = fmaf(Rl, uxf, oxf);
-            X1 = fmaf(Rl, uyf, oyf);
-            X2 = fmaf(Rl, uzf, ozf);
-            R2 = fmaf(X0, X0, fmaf(X1, X1, X2 * X2));
-            rinv = rsqrt_ftz(R2);
-            if (type == ZL_CLOUD || type == ZL_BAND) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
-            R = R2 * rinv;
-            lg2R = lg2_ftz(R);
-            Tn = ex2_ftz(P.neg_delta * lg2R);
-            T = P.T0 * Tn;
-#pragma unroll
-            for (int s = 0; s < NSPEC; ++s) {
-              const float2 bd = bb_lookup_d(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
-              Bv[s] = bd.x;
-              dB[s] = bd.y;
-            }
-            if (SCAT) {
-              theta = atan2f(bperp, -(Rl + beta_h.hi));
-              flux = rinv * rinv;
-#pragma unroll
-              for (int s = 0; s < NSPEC; ++s) {
-                const KSpecF32& S = P.spec[s];
-                eC3[s] = ex2_ftz(S.C3l2e * theta);
-                base[s] = S.C1 + S.C2 * theta + eC3[s];
-                sf[s] = S.S * flux * (S.N * base[s]);
-              }
-            }
-          }
-          // component frame: X - X_0, its norm, height above the symmetry plane
-          const float Xc0 = X0 - C.ox, Xc1 = X1 - C.oy, Xc2 = X2 - C.oz;
-          float Rc2 = R2, rcinv = rinv, Rc = R, lg2Rc = lg2R;
-          if (Fl::offset(C, c)) {
-            Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
-            rcinv = rsqrt_ftz(Rc2);
-            if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
-            Rc = Rc2 * rcinv;
-            lg2Rc = 0.5f * lg2_ftz(Rc2);
-          }
-          const float Z = fmaf(Rl, un_c[c], on_c[c]);
-          const float aZ = fabsf(Z);
-          const float* q = A.q[c];
-          // density = n_0 du; GR = d ln n / d R_c, GZ = d ln n / d Z; p6.. = d ln n / d (own params)
-          float du, GR, GZ, p6 = 0.f, p7 = 0.f, p8 = 0.f, p9 = 0.f, p10 = 0.f, dthx = 0.f, dthy = 0.f;
-          if (type == ZL_CLOUD) {
-            // q: alpha, beta, gamma, mu, 1/mu
-            const float zeta = aZ * rcinv;
-            const bool in = zeta < q[3];
-            const float g = in ? zeta * zeta * C.c[5] : zeta - C.c[6];
-            const float lgg = lg2_ftz(g);
-            const float gg = ex2_ftz(q[2] * lgg);
-            du = ex2_ftz(-q[0] * lg2Rc - C.c[2] * gg);
-            const float bgg = q[1] * q[2] * gg;
-            // one reciprocal: 2 / zeta inside the widening (in), 1 / g outside (g > 0 where used)
-            const float rg = __fdividef(1.f, in ? 0.5f * zeta : g);
-            const float Az = zeta > 0.f ? bgg * rg : 0.f;
-            GR = (-q[0] + Az * zeta) * rcinv;
-            GZ = -copysignf(Az, Z) * rcinv;
-            p6 = -lg2Rc * kLn2;
-            p7 = -gg;
-            p8 = g > 0.f ? -q[1] * gg * lgg * kLn2 : 0.f;
-            p9 = in ? bgg * q[4] : (g > 0.f ? 0.5f * bgg * rg : 0.f);
-          } else if (type == ZL_BAND) {
-            // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
-            const float x = aZ * rcinv * C.c[1];
-            const float x2 = x * x, x6 = x2 * x2 * x2;
-            const float t2 = ex2_ftz(-kLog2e * x6);
-            const float lgx = lg2_ftz(x);
-            const float xp = Fl::p4(C, c) ? x2 * x2 : ex2_ftz(q[2] * lgx);
-            const float xpv = xp * C.c[2];
-            const float t3 = 1.f + xpv;
-            float t4 = 0.f, Y4 = 0.f;
-            bool shared = false;
-            if (Fl::runtime) {
-#pragma unroll
-              for (int j = 0; j < NC; ++j)
-                if (j < c && C.share_t4 == j && ((MASK >> j) & 1u)) {
-                  t4 = t4s[j];
-                  Y4 = y4s[j];
-                  shared = true;
-                }
-            } else if (Fl::share_first(c) && ((MASK >> L::first_band(c)) & 1u)) {
-              t4 = t4s[L::first_band(c)];
-              Y4 = y4s[L::first_band(c)];
-              shared = true;
-            }
-            if (!shared) {
-              const float qq = Rc2 * C.c[4];
-              const float qq2 = qq * qq, qq4 = qq2 * qq2, qq8 = qq4 * qq4;
-              const float y = qq8 * qq2;
-              const float emy = ex2_ftz(-kLog2e * y);
-              t4 = y < 0.25f ? y * (1.f - y * (0.5f - y * (1.f / 6.f - y * (1.f / 24.f - y * (1.f / 120.f - y * (1.f / 720.f))))))
-                             : 1.f - emy;
-              Y4 = t4 > 0.f ? y * emy * __fdividef(1.f, t4) : 1.f;  // y d ln(1 - e^-y) / d y
-            }
-            t4s[c] = t4;
-            y4s[c] = Y4;
-            du = rcinv * t2 * t3 * t4;  // the factor 3 of 3 n_0 is in A.n0 (and in d/dn_0 below)
-            const float it3 = __fdividef(1.f, t3);
-            const float Sx = -6.f * x6 + q[2] * xpv * it3;  // x d ln n / d x
-            GR = (-1.f - Sx + 20.f * Y4) * rcinv;
-            GZ = aZ > 0.f ? __fdividef(Sx, Z) : 0.f;  // Sx sign(Z) / |Z|
-            p6 = -Sx * q[4];
-            p7 = -xpv * it3 * C.c[2];
-            p8 = x > 0.f ? xpv * lgx * kLn2 * it3 : 0.f;
-            p9 = Y4 * q[5];
-          } else {
-            // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
-            float dR = Rc - q[0];
-            const ff hs = hs_r[L::range(c)];
-            const float D2 = fmaf(lin_ff(hs, xk, wa_c[c]), lin_ff(hs, xk, wb_c[c]), rr_c[c]);
-            dR = dR + (D2 - dR * (Rc + q[0])) * (0.5f * rcinv);
-            float arg = dR * dR * q[1] + aZ * q[2];
-            GR = -2.f * dR * q[1];
-            GZ = Z != 0.f ? -copysignf(q[2], Z) : 0.f;
-            p6 = 2.f * dR * q[1];  // d/d R
-            p7 = dR * dR * q[3];   // d/d sigma_r = 2 dR^2 / sigma_r^3
-            p8 = aZ * q[4];        // d/d sigma_z = |Z| / sigma_z^2
-            if (type == ZL_FEATURE) {
-              const float dth = atan2f(fmaf(Rl, ruy[c], roy[c]), fmaf(Rl, rux[c], rox[c]));
-              arg = fmaf(dth * dth, q[5], arg);
-              const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
-              p9 = -gth * kDeg;                     // dtheta/dtheta_deg = -pi/180
-              p10 = dth * dth * q[6];               // 2 dth^2 / sigma_theta^3 per degree
-              const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
-              dthx = gth * (Xc1 * rr - eqx[c]);
-              dthy = gth * (-Xc0 * rr - eqy[c]);
-            }
-            du = ex2_ftz(-kLog2e * arg);
-          }
-          // emission per spectral set and its upstream-weighted sums
-          // E = sum_s g_s e_s and Q = sum_s g_s em1_s dB_s/dT.  With one spectral set and no
-          // scattering both are K B and K dB/dT with K = g em1 constant over the pixel's nodes:
-          // then the sums below run without K and the pixel's K scales them after the loop.
-          float E = 0.f, Q = 0.f;
-          if (!KF) {
-#pragma unroll
-            for (int s = 0; s < NSPEC; ++s) {
-              const KSpecF32& S = P.spec[s];
-              const float ev = SCAT ? fmaf(S.alb[c], sf[s], S.em1[c] * Bv[s]) : S.em1[c] * Bv[s];
-              E = fmaf(gup[c][s], ev, E);
-              Q = fmaf(gup[c][s] * S.em1[c], dB[s], Q);
-            }
-          }
-          const float wdu = wk * du;        // w * density / n_0
-          const float wd = wdu * A.n0[c];  // w * density; the upstream gradient is in E and Q
-          const float coef = KF ? wd * Bv[0] : wd * E;
-          const int o = G::off(c);
-          const float gRr = GR * rcinv;
-          const float cG = coef * gRr, cZ = coef * GZ;
-          acc[o + 0] = fmaf(cG, Rl, acc[o + 0]);  // sum coef g_R R_los
-          acc[o + 1] += cG;                       // sum coef g_R
-          acc[o + 2] += cZ;                       // sum coef g_Z
-          acc[o + 3] = fmaf(cZ, Rl, acc[o + 3]);  // sum coef g_Z R_los
-          if (type == ZL_FEATURE) {
-            fthx[c] = fmaf(coef, dthx, fthx[c]);
-            fthy[c] = fmaf(coef, dthy, fthy[c]);
-          }
-          acc[o + 5] = fmaf(wdu, KF ? Bv[0] : E, acc[o + 5]);
-          acc[o + 6] += coef * p6;
-          acc[o + 7] += coef * p7;
-          acc[o + 8] += coef * p8;
-          if (type != ZL_RING) acc[o + 9] += coef * p9;
-          if (type == ZL_FEATURE) acc[o + 10] += coef * p10;
-          wq = KF ? fmaf(wd, kpix[c], wq) : fmaf(wd, Q, wq);
-          if (last_of_range<LAYOUT, MASK>(c)) {
-            if (KF) wq *= dB[0];
-            acc[G::T0] = fmaf(wq, Tn, acc[G::T0]);
-            acc[G::DELTA] = fmaf(-wq * T, lg2R * kLn2, acc[G::DELTA]);
-            wq = 0.f;
-          }
-#pragma unroll
-          for (int s = 0; s < NSPEC; ++s) {
-            const KSpecF32& S = P.spec[s];
-            // per node only sum w n B and w n S_flux; the pixel's constant factors follow the loop
-            acc[G::eps(c, s)] = fmaf(wd, Bv[s], acc[G::eps(c, s)]);
-            if (SCAT) acc[G::alb(c, s)] = fmaf(wd, sf[s], acc[G::alb(c, s)]);
-            if (SCAT) {
-              const float wg = wd * gup[c][s];
-              const float af = wg * S.alb[c] * flux;
-              acc[G::C(3, s)] += af * S.N * base[s];
-              const float as = af * S.S;
-              acc[G::C(0, s)] += as * (S.N + base[s] * A.dN[s][0]);
-              acc[G::C(1, s)] += as * (S.N * theta + base[s] * A.dN[s][1]);
-              acc[G::C(2, s)] += as * (S.N * theta * eC3[s] + base[s] * A.dN[s][2]);
-            }
-          }
+          if (L::first(c))
+            node_range<NSPEC, SCAT>(P, B, L::range(c), type == ZL_CLOUD || type == ZL_BAND, xk, tab_sm, nT, N);
+          const CompTerms t = comp_terms<LAYOUT, MASK, FLAGS>(c, P, A, B, xk, N, t4s, y4s);
+          comp_accumulate<LAYOUT, MASK, NSPEC, SCAT>(c, P, A, B, wk, N, t, kpix, wq, fthx, fthy, acc);
         }
       }
-
-      // d/dx_0..z_0 = -sum coef g_R (X - X_0)/R - n sum coef g_Z (+ the feature's longitude term);
-      // d/di, d/dOmega = sum coef g_Z (X - X_0) . dn;
-      // d/d eps = g (1 - A) sum w n B,  d/d A = g (sum w n S_flux - eps sum w n B)
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        if (!((MASK >> c) & 1u)) continue;
-        const KCompF32& C = P.comp[c];
-        const int o = G::off(c);
-#pragma unroll
-        for (int s = 0; s < NSPEC; ++s) {
-          const float sB = acc[G::eps(c, s)], sS = SCAT ? acc[G::alb(c, s)] : 0.f;
-          acc[G::eps(c, s)] = gup[c][s] * A.one_m_alb[s][c] * sB;
-          acc[G::alb(c, s)] = gup[c][s] * fmaf(-A.eps[s][c], sB, sS);
-        }
-        // with KF the coefficient sums lack the pixel factor K = g em1 (see the node loop)
-        const float kf = KF ? kpix[c] : 1.f;
-        if (KF) {
-#pragma unroll
-          for (int j = 5; j < G::npar(L::type(c)); ++j) acc[o + j] *= kf;
-          fthx[c] *= kf;
-          fthy[c] *= kf;
-        }
-        if (L::type(c) == ZL_BAND) acc[o + 5] *= 3.f;  // d/dn_0 of 3 n_0 (...)
-        const float s1 = kf * acc[o + 0], s2 = kf * acc[o + 1], s3 = kf * acc[o + 2], s4 = kf * acc[o + 3];
-        const float dxc = oxf - C.ox, dyc = oyf - C.oy, dzc = ozf - C.oz;
-        acc[o + 0] = -fmaf(uxf, s1, dxc * s2) - C.nx * s3 + fthx[c];
-        acc[o + 1] = -fmaf(uyf, s1, dyc * s2) - C.ny * s3 + fthy[c];
-        acc[o + 2] = -fmaf(uzf, s1, dzc * s2) - C.nz * s3;
-        const float ui = uxf * A.dni[c][0] + uyf * A.dni[c][1] + uzf * A.dni[c][2];
-        const float di = dxc * A.dni[c][0] + dyc * A.dni[c][1] + dzc * A.dni[c][2];
-        const float uO = uxf * A.dnO[c][0] + uyf * A.dnO[c][1];
-        const float dO = dxc * A.dnO[c][0] + dyc * A.dnO[c][1];
-        acc[o + 3] = fmaf(ui, s4, di * s3);
-        acc[o + 4] = fmaf(uO, s4, dO * s3);
-      }
+      bwd_finalize<LAYOUT, MASK, NSPEC, SCAT>(P, A, B, kpix, fthx, fthy, acc);
     }
-
-    // ---- tile reduction: fixed shuffle tree, then warps in order ------------
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < NG; ++j) {
-      float v = acc[j];
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-      if (lane == 0) red_sm[warp][j] = v;
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < NG; j += blockDim.x) {
-      double s = 0.0;
-#pragma unroll
-      for (int w = 0; w < kTile / 32; ++w) s += (double)red_sm[w][j];
-      partials[tile * NG + j] = s;
-    }
-    __syncthreads();
+    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, partials, tile);
   }
 }
 
