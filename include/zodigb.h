@@ -305,6 +305,11 @@ ZL_API int zl_debug_one_pixel(int32_t on);
 ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int32_t sink_len,
                               double* ops_per_launch, void* stream);
 
+/* Diagnostics: out[i] = the kernels' branch-free float32 atan2(y[i], x[i]) (the
+ * per-node angle of the feature and of scattering), n device floats each, on
+ * `stream`.  For checking it against a reference atan2. */
+ZL_API int zl_diag_atan2(const float* y_dev, const float* x_dev, float* out_dev, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

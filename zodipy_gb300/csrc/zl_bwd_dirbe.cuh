@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         }
         float2 theta = bc2(0.f), flux = bc2(0.f), eC3[NSPEC], base[NSPEC], sf[NSPEC];
         if (SCAT) {  // scattering.py:11-59
-          theta = make_float2(atan2f(B.bperp, -(Rl.x + B.beta_h.hi)), atan2f(B.bperp, -(Rl.y + B.beta_h.hi)));
+          theta = make_float2(atan2_poly(B.bperp, -(Rl.x + B.beta_h.hi)),
+                              atan2_poly(B.bperp, -(Rl.y + B.beta_h.hi)));
           flux = mul2(rinv, rinv);
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) {
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         const float2 p7 = mul2(dR2, q3);  // d/d sigma_r
         const float2 p8 = mul2(aZ, q4);   // d/d sigma_z
         // the feature's longitude term (lane .y)
-        const float dth = atan2f(fmaf(Rl.y, B.ruy[CF], B.roy[CF]), fmaf(Rl.y, B.rux[CF], B.rox[CF]));
+        const float dth = atan2_poly(fmaf(Rl.y, B.ruy[CF], B.roy[CF]), fmaf(Rl.y, B.rux[CF], B.rox[CF]));
         const float dth2 = dth * dth;
         arg.y = fmaf(dth2, A.q[CF][5], arg.y);
         const float gth = -2.f * dth * A.q[CF][5];  // d ln n / d dtheta

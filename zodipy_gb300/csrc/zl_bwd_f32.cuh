@@ -227,7 +227,7 @@ __device__ __forceinline__ void node_range(const KParamsF32& P, const BwdPix<NC,
 #pragma unroll
   for (int s = 0; s < NSPEC; ++s) N.sf[s] = N.base[s] = N.eC3[s] = 0.f;
   if (SCAT) {
-    N.theta = atan2f(B.bperp, -(N.Rl + B.beta_h.hi));
+    N.theta = atan2_poly(B.bperp, -(N.Rl + B.beta_h.hi));
     N.flux = N.rinv * N.rinv;
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s) {
@@ -345,7 +345,7 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
     t.p7 = dR * dR * q[3];   // d/d sigma_r = 2 dR^2 / sigma_r^3
     t.p8 = aZ * q[4];        // d/d sigma_z = |Z| / sigma_z^2
     if (type == ZL_FEATURE) {
-      const float dth = atan2f(fmaf(N.Rl, B.ruy[c], B.roy[c]), fmaf(N.Rl, B.rux[c], B.rox[c]));
+      const float dth = atan2_poly(fmaf(N.Rl, B.ruy[c], B.roy[c]), fmaf(N.Rl, B.rux[c], B.rox[c]));
       arg = fmaf(dth * dth, q[5], arg);
       const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
       t.p9 = -gth * kDeg;                   // dtheta/dtheta_deg = -pi/180

@@ -211,6 +211,38 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// atan2(y, x) without branches, for the per-node angles of the float32 kernels (the
+// feature's longitude offset, the scattering angle).  Octant reduction: with
+// t = min(|x|, |y|) / max(|x|, |y|) in [0, 1] (one rcp.approx), atan t = t + t^3 Q(t^2)
+// with Q of degree 7, its coefficients fitted for this library by iteratively reweighted
+// least squares (Lawson's method) on the relative error of atan over [0, 1] (1.1 ulp
+// there in float32); then atan2 = pi/2 - atan t where |y| > |x|, pi - (that) where
+// x < 0, and the sign of y.  About 3 ulp from the correctly rounded atan2 for finite
+// arguments; (0, 0) gives 0.
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(fmaxf(ax, ay), 1e-37f), mn = fminf(ax, ay);
+  const float t = mn * rcp_ftz(mx);
+  const float s = t * t;
+  float q = 0.0029206655f;
+  q = fmaf(q, s, -0.016367827f);
+  q = fmaf(q, s, 0.043211706f);
+  q = fmaf(q, s, -0.07552202f);
+  q = fmaf(q, s, 0.10665999f);
+  q = fmaf(q, s, -0.14211054f);
+  q = fmaf(q, s, 0.19993773f);
+  q = fmaf(q, s, -0.33333153f);
+  float r = fmaf(t * s, q, t);
+  r = ay > ax ? 1.5707964f - r : r;
+  r = x < 0.f ? 3.1415927f - r : r;
+  return copysignf(r, y);
+}
 
 // ---------------------------------------------------------------------------
 // Binary search of the observer that owns pixel `i` (records sorted by pix_begin).

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/zodigb.h"
+#include "zl_common.cuh"
 
 namespace {
 
@@ -63,7 +64,21 @@ __global__ void __launch_bounds__(256) fma2_probe(float* sink, int iters, float 
   if (s == 1234.5f) sink[blockIdx.x] = s;
 }
 
+__global__ void atan2_eval(const float* __restrict__ y, const float* __restrict__ x, float* __restrict__ out,
+                           int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = zl::atan2_poly(y[i], x[i]);
+}
+
 }  // namespace
+
+extern "C" ZL_API int zl_diag_atan2(const float* y_dev, const float* x_dev, float* out_dev, int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && (!y_dev || !x_dev || !out_dev))) return ZL_ERR_ARG;
+  if (n == 0) return ZL_OK;
+  const int64_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  atan2_eval<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(y_dev, x_dev, out_dev, n);
+  return cudaGetLastError() == cudaSuccess ? ZL_OK : ZL_ERR_CUDA;
+}
 
 extern "C" ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int32_t sink_len,
                                          double* ops_per_launch, void* stream) {

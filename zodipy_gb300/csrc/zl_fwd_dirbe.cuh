@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
         wS0[s] = 0.f;
       }
       if (Fl::scat(P)) {  // scattering.py:11-59
-        const float theta = atan2f(PS.bperp, -wh);
+        const float theta = atan2_poly(PS.bperp, -wh);
         const float flux = rinv * rinv;
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
           wSq[s] = bc2(0.f);
         }
         if (Fl::scat(P)) {
-          const float2 theta = make_float2(atan2f(PS.bperp, -whq.x), atan2f(PS.bperp, -whq.y));
+          const float2 theta = make_float2(atan2_poly(PS.bperp, -whq.x), atan2_poly(PS.bperp, -whq.y));
           const float2 flux = mul2(rinvq, rinvq);
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) {
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
         dR = fma2(fma2(dR, nt, D2), mul2(bc2(0.5f), rinvq), dR);
         const float2 Z = lin_ff_x2(z1q, xk, z0q);
         float2 arg = fma2(mul2(dR, dR), cpair(Cr, Cf, 2), mul2(abs2(Z), cpair(Cr, Cf, 3)));
-        const float dth = atan2f(fmaf(PS.fy1[5], xk.hi, PS.fy0[5]), fmaf(PS.fx1[5], xk.hi, PS.fx0[5]));
+        const float dth = atan2_poly(fmaf(PS.fy1[5], xk.hi, PS.fy0[5]), fmaf(PS.fx1[5], xk.hi, PS.fx0[5]));
         arg.y = fmaf(dth * dth, Cf.c[7], arg.y);
         const float2 dens = make_float2(ex2_ftz(-arg.x), ex2_ftz(-arg.y));
 #pragma unroll

@@ -21,7 +21,8 @@
 //    keep float32 relative accuracy where R^-alpha is steepest;
 //  - everything else runs in float32 with single MUFU instructions (ex2, lg2,
 //    rsqrt), integer powers by squaring and 1 - e^-y by its series where it
-//    would cancel;
+//    would cancel; the per-node angles (the feature's longitude offset, the
+//    scattering angle) use a branch-free polynomial atan2 (atan2_poly, ~3 ulp);
 //  - each component's quadrature sum is Kahan-compensated in float32 and
 //    written as float64.
 // One thread integrates one pixel over all nodes and components in node order,
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) wB[s] = wk * bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
           if (Fl::scat(P)) {  // scattering.py:11-59
-            const float theta = atan2f(bperp, -wh);
+            const float theta = atan2_poly(bperp, -wh);
             const float flux = rinv * rinv;
 #pragma unroll
             for (int s = 0; s < NSPEC; ++s) {
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           }
           float arg = dR * dR * C.c[2] + fabsf(Z) * C.c[3];
           if (featurelike(type)) {
-            const float dth = atan2f(fmaf(fy1[c], xk.hi, fy0[c]), fmaf(fx1[c], xk.hi, fx0[c]));
+            const float dth = atan2_poly(fmaf(fy1[c], xk.hi, fy0[c]), fmaf(fx1[c], xk.hi, fx0[c]));
             arg = fmaf(dth * dth, C.c[7], arg);
           }
           dens = ex2_ftz(-arg);

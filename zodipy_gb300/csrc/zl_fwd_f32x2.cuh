@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
             wB[s] = mul2(bc2(wk), make_float2(bb_lookup(tab_sm + s * nT, T.x, P.t_min, P.t_max, P.inv_dt, nT),
                                               bb_lookup(tab_sm + s * nT, T.y, P.t_min, P.t_max, P.inv_dt, nT)));
           if (Fl::scat(P)) {  // scattering.py:11-59
-            const float2 theta = make_float2(atan2f(bperp.x, -wh.x), atan2f(bperp.y, -wh.y));
+            const float2 theta = make_float2(atan2_poly(bperp.x, -wh.x), atan2_poly(bperp.y, -wh.y));
             const float2 flux = mul2(rinv, rinv);
 #pragma unroll
             for (int s = 0; s < NSPEC; ++s) {
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
           if (featurelike(type)) {
             const float2 yy = fma2(fy1[c], bc2(xk.hi), fy0[c]);
             const float2 xx = fma2(fx1[c], bc2(xk.hi), fx0[c]);
-            const float2 dth = make_float2(atan2f(yy.x, xx.x), atan2f(yy.y, xx.y));
+            const float2 dth = make_float2(atan2_poly(yy.x, xx.x), atan2_poly(yy.y, xx.y));
             arg = fma2(mul2(dth, dth), bc2(C.c[7]), arg);
           }
           dens = make_float2(ex2_ftz(-arg.x), ex2_ftz(-arg.y));
