@@ -222,7 +222,7 @@ __device__ __forceinline__ float rcp_ftz(float x) {
 // t = min(|x|, |y|) / max(|x|, |y|) in [0, 1] (one rcp.approx), atan t = t + t^3 Q(t^2)
 // with Q of degree 7, its coefficients fitted for this library by iteratively reweighted
 // least squares (Lawson's method) on the relative error of atan over [0, 1] (1.1 ulp
-// there in float32); then atan2 = pi/2 - atan t where |y| > |x|, pi - (that) where
+// there in float32; fit_atan2_poly.py beside this file reproduces them); then atan2 = pi/2 - atan t where |y| > |x|, pi - (that) where
 // x < 0, and the sign of y.  About 3 ulp from the correctly rounded atan2 for finite
 // arguments; (0, 0) gives 0.
 __device__ __forceinline__ float atan2_poly(float y, float x) {
