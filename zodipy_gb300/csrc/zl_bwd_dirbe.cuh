@@ -72,7 +72,6 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
       const float2 unP = make_float2(B.un_c[CR], B.un_c[CF]), onP = make_float2(B.on_c[CR], B.on_c[CF]);
       // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
       const float2 q0 = qpair(A, CR, CF, 0), q1 = qpair(A, CR, CF, 1), q2 = qpair(A, CR, CF, 2);
-      const float2 q3 = qpair(A, CR, CF, 3), q4 = qpair(A, CR, CF, 4);
       const float2 nq0 = mul2(q0, bc2(-1.f)), m2q1 = mul2(q1, bc2(-2.f));
       const float2 n0P = make_float2(A.n0[CR], A.n0[CF]);
       // per spectral set: g em1 and g alb of each lane (E and Q below)
@@ -88,9 +87,9 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
 #pragma unroll
       for (int c = 0; c < NC; ++c) kpix[c] = KF ? B.gup[c][0] * P.spec[0].em1[c] : 0.f;
 
-      // node sums: the scalar kernel's acc[off + j] per lane (s6n = -acc[off + 6]); T_0 and
+      // node sums: the scalar kernel's acc[off + j] per lane (before comp_pfactors); T_0 and
       // delta per lane without the factor K (KF) and -ln 2 (delta)
-      float2 s0 = bc2(0.f), s1 = bc2(0.f), s2 = bc2(0.f), s3 = bc2(0.f), s5 = bc2(0.f), s6n = bc2(0.f);
+      float2 s0 = bc2(0.f), s1 = bc2(0.f), s2 = bc2(0.f), s3 = bc2(0.f), s5 = bc2(0.f), s6 = bc2(0.f);
       float2 s7 = bc2(0.f), s8 = bc2(0.f), sT0 = bc2(0.f), sD = bc2(0.f);
       float s9 = 0.f, s10 = 0.f, fx = 0.f, fy = 0.f;
       float2 sE[NSPEC], sA[NSPEC], sC[4][NSPEC];
@@ -148,14 +147,11 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         float2 arg = fma2(dR2, q1, mul2(aZ, q2));
         const float2 GR = mul2(dR, m2q1);  // d ln n / d R; d/d R0 is -GR
         const float2 GZ = make_float2(Z.x != 0.f ? -copysignf(q2.x, Z.x) : 0.f, Z.y != 0.f ? -copysignf(q2.y, Z.y) : 0.f);
-        const float2 p7 = mul2(dR2, q3);  // d/d sigma_r
-        const float2 p8 = mul2(aZ, q4);   // d/d sigma_z
         // the feature's longitude term (lane .y)
         const float dth = atan2_poly(fmaf(Rl.y, B.ruy[CF], B.roy[CF]), fmaf(Rl.y, B.rux[CF], B.rox[CF]));
         const float dth2 = dth * dth;
         arg.y = fmaf(dth2, A.q[CF][5], arg.y);
         const float gth = -2.f * dth * A.q[CF][5];  // d ln n / d dtheta
-        const float p9 = -gth * kDeg, p10 = dth2 * A.q[CF][6];
         const float Xc0 = X0.y - Cf.ox, Xc1 = X1.y - Cf.oy;
         const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
         const float dthx = gth * (Xc1 * rr - B.eqx[CF]), dthy = gth * (-Xc0 * rr - B.eqy[CF]);
@@ -175,17 +171,17 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         const float2 wd = mul2(wdu, n0P);
         const float2 coef = mul2(wd, KF ? Bv[0] : E);
         const float2 cGR = mul2(coef, GR);
-        s6n = add2(s6n, cGR);
+        s6 = add2(s6, cGR);
         const float2 cG = mul2(cGR, rinv), cZ = mul2(coef, GZ);
         s0 = fma2(cG, Rl, s0);
         s1 = add2(s1, cG);
         s2 = add2(s2, cZ);
         s3 = fma2(cZ, Rl, s3);
         s5 = fma2(wdu, KF ? Bv[0] : E, s5);
-        s7 = fma2(coef, p7, s7);
-        s8 = fma2(coef, p8, s8);
-        s9 = fmaf(coef.y, p9, s9);
-        s10 = fmaf(coef.y, p10, s10);
+        s7 = fma2(coef, dR2, s7);
+        s8 = fma2(coef, aZ, s8);
+        s9 = fmaf(coef.y, dth, s9);
+        s10 = fmaf(coef.y, dth2, s10);
         fx = fmaf(coef.y, dthx, fx);
         fy = fmaf(coef.y, dthy, fy);
         const float2 wq = mul2(wd, KF ? dB[0] : Q);
@@ -215,7 +211,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
       acc[oR + 2] = s2.x, acc[oF + 2] = s2.y;
       acc[oR + 3] = s3.x, acc[oF + 3] = s3.y;
       acc[oR + 5] = s5.x, acc[oF + 5] = s5.y;
-      acc[oR + 6] = -s6n.x, acc[oF + 6] = -s6n.y;
+      acc[oR + 6] = s6.x, acc[oF + 6] = s6.y;
       acc[oR + 7] = s7.x, acc[oF + 7] = s7.y;
       acc[oR + 8] = s8.x, acc[oF + 8] = s8.y;
       acc[oF + 9] = s9, acc[oF + 10] = s10;
@@ -282,8 +278,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
       // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
       const float2 c1P = make_float2(K1.c[1], K2.c[1]), c2P = make_float2(K1.c[2], K2.c[2]);
       const float2 c4P = make_float2(K1.c[4], K2.c[4]);
-      const float2 q2P = qpair(A, C1, C2, 2), q5P = qpair(A, C1, C2, 5);
-      const float2 mq4P = mul2(qpair(A, C1, C2, 4), bc2(-1.f)), mc2P = mul2(c2P, bc2(-1.f));
+      const float2 q2P = qpair(A, C1, C2, 2);
       const float2 n0P = make_float2(A.n0[C1], A.n0[C2]);
       float2 gq[NSPEC], ga[NSPEC];
 #pragma unroll
@@ -302,7 +297,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
       for (int c = 0; c < NC; ++c) kpix[c] = KF ? B.gup[c][0] * P.spec[0].em1[c] : 0.f;
       const float2 kP = make_float2(kpix[C1], kpix[C2]);
 
-      // bands 1 and 2: the scalar kernel's acc[off + j] per lane
+      // bands 1 and 2: the scalar kernel's acc[off + j] per lane (before comp_pfactors)
       float2 b0 = bc2(0.f), b1 = bc2(0.f), b2 = bc2(0.f), b3 = bc2(0.f), b5 = bc2(0.f);
       float2 b6 = bc2(0.f), b7 = bc2(0.f), b8 = bc2(0.f), b9 = bc2(0.f);
       float2 bE[NSPEC], bA[NSPEC];
@@ -359,11 +354,8 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
           const float2 GR = mul2(sub2(fma2(Y4, bc2(20.f), bc2(-1.f)), Sx), bc2(N.rinv));
           const float2 sz = mul2(Sx, make_float2(__fdividef(1.f, Z.x), __fdividef(1.f, Z.y)));
           const float2 GZ = make_float2(aZ.x > 0.f ? sz.x : 0.f, aZ.y > 0.f ? sz.y : 0.f);
-          const float2 p6 = mul2(Sx, mq4P);
-          const float2 p7 = mul2(xit, mc2P);
-          const float2 p8r = mul2(mul2(xit, lgx), bc2(kLn2));
+          const float2 p8r = mul2(xit, lgx);
           const float2 p8 = make_float2(x.x > 0.f ? p8r.x : 0.f, x.y > 0.f ? p8r.y : 0.f);
-          const float2 p9 = mul2(Y4, q5P);
 
           float2 E = bc2(0.f), Q = bc2(0.f);
           if (!KF) {
@@ -383,10 +375,10 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
           b2 = add2(b2, cZ);
           b3 = fma2(cZ, bc2(N.Rl), b3);
           b5 = fma2(wdu, KF ? bc2(N.Bv[0]) : E, b5);
-          b6 = fma2(coef, p6, b6);
-          b7 = fma2(coef, p7, b7);
+          b6 = fma2(coef, Sx, b6);
+          b7 = fma2(coef, xit, b7);
           b8 = fma2(coef, p8, b8);
-          b9 = fma2(coef, p9, b9);
+          b9 = fma2(coef, Y4, b9);
           const float2 wqp = mul2(wd, KF ? kP : Q);
           wq += wqp.x + wqp.y;
 #pragma unroll

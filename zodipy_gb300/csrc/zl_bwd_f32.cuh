@@ -240,7 +240,8 @@ __device__ __forceinline__ void node_range(const KParamsF32& P, const BwdPix<NC,
 }
 
 // Density of one component at a node (without n_0) and its log-derivatives:
-// GR = d ln n / d R_c, GZ = d ln n / d Z, p6.. = d ln n / d (own parameters).
+// GR = d ln n / d R_c, GZ = d ln n / d Z, p6.. = d ln n / d (own parameters) without
+// their pixel-constant factors, which multiply the node sums once (comp_pfactors).
 struct CompTerms {
   float du, GR, GZ, rcinv, p6, p7, p8, p9, p10, dthx, dthy;
 };
@@ -284,10 +285,11 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
     const float Az = zeta > 0.f ? bgg * rg : 0.f;
     t.GR = (-q[0] + Az * zeta) * rcinv;
     t.GZ = -copysignf(Az, Z) * rcinv;
-    t.p6 = -lg2Rc * kLn2;
-    t.p7 = -gg;
-    t.p8 = g > 0.f ? -q[1] * gg * lgg * kLn2 : 0.f;
-    t.p9 = in ? bgg * q[4] : (g > 0.f ? 0.5f * bgg * rg : 0.f);
+    // outside the widening g = zeta - mu/2 > 0 and zeta > 0, so d/dmu there is Az / 2
+    t.p6 = lg2Rc;                            // d/d alpha = -ln 2 lg2 R
+    t.p7 = gg;                               // d/d beta = -g^gamma
+    t.p8 = g > 0.f ? gg * lgg : 0.f;         // d/d gamma = -beta ln 2 g^gamma lg2 g
+    t.p9 = in ? bgg * (2.f * q[4]) : Az;     // d/d mu (x 1/2)
   } else if (type == ZL_BAND) {
     // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
     const float x = aZ * rcinv * C.c[1];
@@ -325,13 +327,14 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
     y4s[c] = Y4;
     t.du = rcinv * t2 * t3 * t4;  // the factor 3 of 3 n_0 is in A.n0 (and in d/dn_0 below)
     const float it3 = __fdividef(1.f, t3);
-    const float Sx = -6.f * x6 + q[2] * xpv * it3;  // x d ln n / d x
+    const float xit = xpv * it3;
+    const float Sx = -6.f * x6 + q[2] * xit;  // x d ln n / d x
     t.GR = (-1.f - Sx + 20.f * Y4) * rcinv;
     t.GZ = aZ > 0.f ? __fdividef(Sx, Z) : 0.f;  // Sx sign(Z) / |Z|
-    t.p6 = -Sx * q[4];
-    t.p7 = -xpv * it3 * C.c[2];
-    t.p8 = x > 0.f ? xpv * lgx * kLn2 * it3 : 0.f;
-    t.p9 = Y4 * q[5];
+    t.p6 = Sx;                                   // d/d delta_zeta = -Sx / delta_zeta
+    t.p7 = xit;                                  // d/d v = -xit / v
+    t.p8 = x > 0.f ? xit * lgx : 0.f;            // d/d p = ln 2 xit lg2 x
+    t.p9 = Y4;                                   // d/d delta_r = -20 Y4 / delta_r
   } else {
     // q: R, 1/sigma_r^2, 1/sigma_z, 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3
     float dR = Rc - q[0];
@@ -341,15 +344,15 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
     float arg = dR * dR * q[1] + aZ * q[2];
     t.GR = -2.f * dR * q[1];
     t.GZ = Z != 0.f ? -copysignf(q[2], Z) : 0.f;
-    t.p6 = 2.f * dR * q[1];  // d/d R
-    t.p7 = dR * dR * q[3];   // d/d sigma_r = 2 dR^2 / sigma_r^3
-    t.p8 = aZ * q[4];        // d/d sigma_z = |Z| / sigma_z^2
+    t.p6 = t.GR;             // d/d R = -GR
+    t.p7 = dR * dR;          // d/d sigma_r = 2 dR^2 / sigma_r^3
+    t.p8 = aZ;               // d/d sigma_z = |Z| / sigma_z^2
     if (type == ZL_FEATURE) {
       const float dth = atan2_poly(fmaf(N.Rl, B.ruy[c], B.roy[c]), fmaf(N.Rl, B.rux[c], B.rox[c]));
       arg = fmaf(dth * dth, q[5], arg);
       const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
-      t.p9 = -gth * kDeg;                   // dtheta/dtheta_deg = -pi/180
-      t.p10 = dth * dth * q[6];             // 2 dth^2 / sigma_theta^3 per degree
+      t.p9 = dth;                           // d/d theta = -gth pi/180 = 2 dth pi/180 / sigma_theta^2
+      t.p10 = dth * dth;                    // d/d sigma_theta = 2 dth^2 / sigma_theta^3 per degree
       const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
       t.dthx = gth * (Xc1 * rr - B.eqx[c]);
       t.dthy = gth * (-Xc0 * rr - B.eqy[c]);
@@ -429,6 +432,21 @@ __device__ __forceinline__ void comp_accumulate(int c, const KParamsF32& P, cons
   }
 }
 
+// Pixel-constant factors of the node sums acc[off + 6 ..] (comp_terms returns the
+// log-derivatives without them).
+// q: cloud alpha, beta, gamma, mu, 1/mu; band delta_zeta [deg], v, p, delta_r,
+// 1/delta_zeta [deg], -20/delta_r; ring/feature R, 1/sigma_r^2, 1/sigma_z,
+// 2/sigma_r^3, 1/sigma_z^2, 1/sigma_theta^2, 2 deg/sigma_theta^3.
+__device__ __forceinline__ void comp_pfactors(int type, const float* q, const KCompF32& C, float (&f)[5]) {
+  if (type == ZL_CLOUD) {
+    f[0] = -kLn2, f[1] = -1.f, f[2] = -q[1] * kLn2, f[3] = 0.5f, f[4] = 0.f;
+  } else if (type == ZL_BAND) {
+    f[0] = -q[4], f[1] = -C.c[2], f[2] = kLn2, f[3] = q[5], f[4] = 0.f;
+  } else {
+    f[0] = -1.f, f[1] = q[3], f[2] = q[4], f[3] = 2.f * q[5] * kDeg, f[4] = q[6];
+  }
+}
+
 // After the node loop: d/dx_0..z_0 = -sum coef g_R (X - X_0)/R - n sum coef g_Z (+ the
 // feature's longitude term); d/di, d/dOmega = sum coef g_Z (X - X_0) . dn;
 // d/d eps = g (1 - A) sum w n B,  d/d A = g (sum w n S_flux - eps sum w n B).
@@ -443,6 +461,12 @@ __device__ __forceinline__ void bwd_finalize(const KParamsF32& P, const KGradAux
     if (!((MASK >> c) & 1u)) continue;
     const KCompF32& C = P.comp[c];
     const int o = G::off(c);
+    {
+      float f[5];
+      comp_pfactors(L::type(c), A.q[c], C, f);
+#pragma unroll
+      for (int j = 6; j < G::npar(L::type(c)); ++j) acc[o + j] *= f[j - 6];
+    }
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s) {
       const float sB = acc[G::eps(c, s)], sS = SCAT ? acc[G::alb(c, s)] : 0.f;
