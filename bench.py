@@ -62,7 +62,7 @@ def parse():
     p.add_argument("--large-nside", type=int, default=2048)
     p.add_argument(
         "--profile-case",
-        choices=["fwd", "bwd", "fwd-planck"],
+        choices=["fwd", "bwd", "fwd-planck", "fwd64"],
         help="only run a few launches of one kernel of the workload (a target for ncu captures); no JSON",
     )
     return p.parse_args()
@@ -352,7 +352,7 @@ def profile_case(args):
 
         model = zg.Model(857 * un.GHz, name="planck18", precision="float32")
     else:
-        model = build_model("float32")
+        model = build_model("float64" if args.profile_case == "fwd64" else "float32")
     zl = model.zl_model
     u = torch.from_numpy(u_np).cuda()
     tab = packing.observer_table(zl, obs, earth, [0], any_mode=False)
@@ -361,6 +361,8 @@ def profile_case(args):
     for _ in range(max(args.steps, 1)):
         if args.profile_case == "bwd":
             engine.backward(zl, u, obs_dev, 1, g_total=g)
+        elif args.profile_case == "fwd64":
+            engine.forward(zl, u, obs_dev, 1, "float64")
         else:
             engine.forward(zl, u, obs_dev, 1, "float32")
     torch.cuda.synchronize()
