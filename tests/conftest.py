@@ -102,3 +102,28 @@ def lib():
 
     _build.build()
     return _lib.load()
+
+
+def band_tail_share(u, obs, degree=50, warp=32):
+    """Share of (warp of consecutive pixels, quadrature node) pairs at which DIRBE bands 1 and 2
+    are both beyond 2.2 delta_zeta of their planes for every pixel of the warp: the nodes the
+    DIRBE-layout kernels skip as exactly zero.  float64 geometry of the cloud/band LOS range
+    (observer to the 5.2 AU sphere); tells a test that its inputs exercise the skip."""
+    from zodipy_gb300 import model_data
+    from zodipy_gb300.components import ComponentLabel as L
+
+    x, _ = np.polynomial.legendre.leggauss(degree)
+    b = u.T @ obs
+    stop = -b + np.sqrt(b * b - (obs @ obs - 5.2**2))
+    n_w = u.shape[1] // warp
+    dead = np.ones((degree, n_w), bool)
+    for lbl in (L.BAND1, L.BAND2):
+        p = model_data.DIRBE_COMPONENTS[lbl][1]
+        i, om = np.radians(p["i"]), np.radians(p["Omega"])
+        nrm = np.array([np.sin(om) * np.sin(i), -np.cos(om) * np.sin(i), np.cos(i)])
+        for k in range(degree):
+            X = obs[:, None] + (0.5 * stop * (x[k] + 1.0))[None, :] * u
+            zeta = np.abs(nrm @ X) / np.linalg.norm(X, axis=0)
+            far = zeta > 2.2 * np.radians(p["delta_zeta"])
+            dead[k] &= far[: n_w * warp].reshape(n_w, warp).all(axis=1)
+    return float(dead.mean())

@@ -230,3 +230,46 @@ def test_paired_adjoint_equals_scalar_kernel(lib, bands, per_comp):
     dev = np.abs(s_got - s_ref) / (np.abs(s_ref) + 1e-7 * np.abs(s_ref).max())
     worst = int(np.argmax(dev))
     assert dev.max() <= 1e-5, f"{names[worst]}: paired {got[worst]:.9e} scalar {ref[worst]:.9e} ({dev.max():.2e})"
+
+
+@pytest.mark.parametrize("bands,per_comp", [((25.0,), False), ((12.0, 25.0, 60.0), False), ((25.0,), True)])
+def test_paired_adjoint_band_tails_healpix_order(lib, bands, per_comp):
+    """The {cloud, bands} adjoint kernel stops evaluating the bands past the node from which
+    they are zero for every pixel of a warp (about half of this HEALPix map's nodes; random
+    directions almost never give such warps).  Against the scalar kernel, which evaluates
+    every node; same metric and tolerance as above."""
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import _lib, engine, packing, params
+    from zodipy_gb300 import units as u_
+    from zodipy_gb300.autograd import fuse_models
+    from zodipy_gb300.healpix import pix2vec_ring
+
+    from conftest import band_tail_share
+
+    models = [zg.Model(b * u_.micron) for b in bands]
+    zl = fuse_models(models)
+    obs_xyz = np.array([0.75, 0.66, 0.01])
+    u_np = pix2vec_ring(32)
+    assert band_tail_share(u_np, obs_xyz) > 0.3
+    dirs = torch.from_numpy(u_np).cuda()
+    tab = packing.observer_table(zl, obs_xyz, [0.76, 0.65, 0.0], [0], any_mode=False)
+    obs = engine.upload_observers(tab)
+    gen = torch.Generator("cuda").manual_seed(7)
+    n = dirs.shape[1]
+    shape = (len(bands), zl.n_comps, n) if per_comp else (len(bands), n)
+    g = 0.5 + torch.rand(shape, dtype=torch.float64, device="cuda", generator=gen)
+    kw = {"g_comps": g} if per_comp else {"g_total": g}
+    try:
+        _lib.check(lib.zl_debug_one_pixel(1), "scalar kernels")
+        ref = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
+    finally:
+        _lib.check(lib.zl_debug_one_pixel(0), "default kernels")
+    got = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
+    names = params.names(zl, models[0].comp_labels)
+    scale = np.maximum(np.abs(params.vector_from_model(zl)), 1.0)
+    s_got, s_ref = got * scale, ref * scale
+    dev = np.abs(s_got - s_ref) / (np.abs(s_ref) + 1e-7 * np.abs(s_ref).max())
+    worst = int(np.argmax(dev))
+    assert dev.max() <= 1e-5, f"{names[worst]}: paired {got[worst]:.9e} scalar {ref[worst]:.9e} ({dev.max():.2e})"

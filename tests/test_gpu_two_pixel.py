@@ -95,3 +95,31 @@ def test_component_paired_equals_one_pixel(lib, bands):
     tab = packing.observer_table(zl, obs, earth, [0], any_mode=False)
     comps, total = engine.forward(zl, torch.from_numpy(dirs).cuda(), engine.upload_observers(tab), 1, "float32")
     _check((comps.cpu().numpy(), total.cpu().numpy()), a)
+
+
+@pytest.mark.parametrize("bands", [(25.0,), (1.25,), (12.0, 25.0, 60.0)])
+def test_component_paired_band_tails_healpix_order(lib, bands):
+    """In HEALPix RING order the 32 pixels of a warp lie on one latitude ring, so beyond some
+    node every pixel of the warp is far enough from the bands' planes that their factor
+    e^-(zeta/dzeta)^6 is zero in float32, and the paired kernel stops evaluating them (about
+    half of this map's nodes; random directions, as above, almost never form such a warp).
+    Same tolerance against the one-pixel kernel, which evaluates every node."""
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import _lib, engine, packing
+    from zodipy_gb300 import units as u_
+    from zodipy_gb300.autograd import fuse_models
+    from zodipy_gb300.healpix import pix2vec_ring
+
+    from conftest import band_tail_share
+
+    zl = fuse_models([zg.Model(b * u_.micron) for b in bands])
+    dirs = pix2vec_ring(64)
+    obs, earth = np.array([0.75, 0.66, 0.01]), np.array([0.76, 0.65, 0.0])
+    assert band_tail_share(dirs, obs) > 0.3
+    ref = _run(zl, dirs, obs, earth, one_pixel=True)
+    _lib.check(lib.zl_debug_one_pixel(0), "default kernel")
+    tab = packing.observer_table(zl, obs, earth, [0], any_mode=False)
+    comps, total = engine.forward(zl, torch.from_numpy(dirs).cuda(), engine.upload_observers(tab), 1, "float32")
+    _check((comps.cpu().numpy(), total.cpu().numpy()), ref)

@@ -237,6 +237,26 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
   }
 }
 
+// Band 1's 1 - e^-y and y d ln(1 - e^-y)/dy (y = (R/delta_r)^20) as lane .x of the packed
+// bands 1/2 code below forms them, operation for operation: band 3 reuses them at nodes where
+// bands 1 and 2 are not evaluated.
+__device__ __forceinline__ void band1_cutoff(float R2, float inv_dr2, float& t4, float& Y4) {
+  const float qq = R2 * inv_dr2;
+  const float qq2 = qq * qq, qq4 = qq2 * qq2, qq8 = qq4 * qq4;
+  const float y = qq8 * qq2;
+  const float emy = ex2_ftz(-kLog2e * y);
+  const float ny = -y;
+  float ser = fmaf(ny, 1.f / 720.f, 1.f / 120.f);
+  ser = fmaf(ny, ser, 1.f / 24.f);
+  ser = fmaf(ny, ser, 1.f / 6.f);
+  ser = fmaf(ny, ser, 0.5f);
+  ser = y * fmaf(ny, ser, 1.f);
+  const float om = 1.f - emy;
+  t4 = y < 0.25f ? ser : om;
+  const float ye = (y * emy) * __fdividef(1.f, t4);
+  Y4 = t4 > 0.f ? ye : 1.f;
+}
+
 // ---------------------------------------------------------------------------
 // {cloud, bands}: cloud and band 3 scalar, bands 1 and 2 in lanes .x / .y
 // ---------------------------------------------------------------------------
@@ -297,6 +317,22 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
       for (int c = 0; c < NC; ++c) kpix[c] = KF ? B.gup[c][0] * P.spec[0].em1[c] : 0.f;
       const float2 kP = make_float2(kpix[C1], kpix[C2]);
 
+      // nodes from k12 (bands 1 and 2) and k3 (band 3) on add exactly nothing for any pixel of
+      // the warp (band_zero_tail); Z = u_n R_los + o_n and R^2 = (R_los + u . X_obs)^2 + b^2.
+      // With scattering the bands' share of the work is too small for the branches to pay.
+      constexpr bool TAIL = !SCAT;
+      int k12 = P.n_nodes, k3 = P.n_nodes;
+      if (TAIL) {
+        const float bt = B.beta_h.hi;
+        const float b2h = fmaxf(fmaf(B.oxf, B.oxf, fmaf(B.oyf, B.oyf, B.ozf * B.ozf)) - bt * bt, 0.f);
+        const float h0 = B.hs_r[0].hi, m0 = B.mid_r[0].hi;
+        auto tail = [&](int c) {
+          return band_zero_tail(B.un_c[c] * h0, fmaf(B.un_c[c], m0, B.on_c[c]), h0, m0 + bt, b2h, P.comp[c].c[1]);
+        };
+        k12 = warp_tail_index(P, fmaxf(tail(C1), tail(C2)));
+        k3 = warp_tail_index(P, tail(C3));
+      }
+
       // bands 1 and 2: the scalar kernel's acc[off + j] per lane (before comp_pfactors)
       float2 b0 = bc2(0.f), b1 = bc2(0.f), b2 = bc2(0.f), b3 = bc2(0.f), b5 = bc2(0.f);
       float2 b6 = bc2(0.f), b7 = bc2(0.f), b8 = bc2(0.f), b9 = bc2(0.f);
@@ -321,7 +357,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
         }
 
         // ---- bands 1 and 2 (number_density.py:99-110) ----------------------------
-        {
+        if (!TAIL || k < k12) {
           const float2 Z = fma2(bc2(N.Rl), unP, onP);
           const float2 aZ = abs2(Z);
           const float2 x = mul2(mul2(aZ, bc2(N.rinv)), c1P);
@@ -399,9 +435,12 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
         }
 
         // ---- band 3 (band 1's inner-cutoff term; flushes the range's T_0 / delta sums)
-        {
+        if (!TAIL || k < k3) {
+          if (TAIL && k >= k12) band1_cutoff(N.R2, K1.c[4], t4s[C1], y4s[C1]);
           const CompTerms t = comp_terms<LAYOUT, MASK, FLAGS>(C3, P, A, B, xk, N, t4s, y4s);
           comp_accumulate<LAYOUT, MASK, NSPEC, SCAT>(C3, P, A, B, wk, N, t, kpix, wq, fthx, fthy, acc);
+        } else {
+          range_flush<LAYOUT, MASK, NSPEC, SCAT>(N, wq, acc);
         }
       }
 

@@ -362,6 +362,18 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
   return t;
 }
 
+// The T_0 / delta sums of a LOS range: wq (sum over the range's components of w n E_T, or
+// of w n K with one spectral set and no scattering) times dT/dT_0 and dT/d delta.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, int NG>
+__device__ __forceinline__ void range_flush(const NodeR<NSPEC>& N, float& wq, float (&acc)[NG]) {
+  using G = GradLay<LAYOUT, NSPEC>;
+  constexpr bool KF = NSPEC == 1 && !SCAT;
+  if (KF) wq *= N.dB[0];
+  acc[G::T0] = fmaf(wq, N.Tn, acc[G::T0]);
+  acc[G::DELTA] = fmaf(-wq * N.T, N.lg2R * kLn2, acc[G::DELTA]);
+  wq = 0.f;
+}
+
 // Node sums of one component.  The emission per spectral set and its upstream-weighted
 // sums E = sum_s g_s e_s and Q = sum_s g_s em1_s dB_s/dT: with one spectral set and no
 // scattering (KF) both are K B and K dB/dT with K = g em1 constant over the pixel's
@@ -408,12 +420,7 @@ __device__ __forceinline__ void comp_accumulate(int c, const KParamsF32& P, cons
   if (type != ZL_RING) acc[o + 9] += coef * t.p9;
   if (type == ZL_FEATURE) acc[o + 10] += coef * t.p10;
   wq = KF ? fmaf(wd, kpix[c], wq) : fmaf(wd, Q, wq);
-  if (last_of_range<LAYOUT, MASK>(c)) {
-    if (KF) wq *= N.dB[0];
-    acc[G::T0] = fmaf(wq, N.Tn, acc[G::T0]);
-    acc[G::DELTA] = fmaf(-wq * N.T, N.lg2R * kLn2, acc[G::DELTA]);
-    wq = 0.f;
-  }
+  if (last_of_range<LAYOUT, MASK>(c)) range_flush<LAYOUT, MASK, NSPEC, SCAT>(N, wq, acc);
 #pragma unroll
   for (int s = 0; s < NSPEC; ++s) {
     const KSpecF32& S = P.spec[s];

@@ -147,6 +147,50 @@ __device__ __forceinline__ ff sq_plus_ff2(ff w, ff c) {
 // a < b for normalised float-float values
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 
+// Where a band stops contributing (Kelsall bands, number_density.py:99-110).  A band's
+// factor e^-(zeta/dzeta)^6 is evaluated as ex2(-log2(e) (zeta/dzeta)^6), and
+// ex2.approx.ftz returns +0 once its result 2^x falls
+// below the smallest normal float (x < -126, i.e. zeta > 2.11 dzeta): from there on the
+// node adds exactly nothing.  Along a line of sight, zeta = |Z|/R with Z = a1 x + a0 and
+// R^2 = (h x + m)^2 + b^2 in the node abscissa x, so zeta > c for
+//   (a1 x + a0)^2 - c^2 ((h x + m)^2 + b^2) > 0,
+// a quadratic whose leading coefficient a1^2 - c^2 h^2 is positive when the direction
+// itself leaves the band (|u . n| > c).  Then every node beyond the larger root is zero.
+// Returns that root for c = 2.2 dzeta (4 % inside the flush threshold, which absorbs the
+// float32 rounding of this estimate and of the node loop's zeta), -inf when the whole line
+// of sight is beyond it, +inf when no tail is guaranteed (and for NaN input).
+__device__ __forceinline__ float band_zero_tail(float a1, float a0, float h, float m, float b2h, float inv_dzeta) {
+  const float c = 2.2f / inv_dzeta;
+  const float c2 = c * c;
+  const float A = a1 * a1 - c2 * (h * h);
+  const float B = 2.f * (a1 * a0 - c2 * (h * m));
+  const float C = a0 * a0 - c2 * (m * m + b2h);
+  if (!(A > 0.f)) return INFINITY;
+  const float disc = B * B - 4.f * A * C;
+  if (disc < 0.f) return -INFINITY;
+  const float q = -0.5f * (B + copysignf(sqrtf(disc), B));
+  const float r = fmaxf(q / A, C / q);  // the two roots; q != 0 here (disc >= 0, A > 0)
+  return isnan(r) ? INFINITY : r;
+}
+
+// Number of quadrature nodes at or below abscissa xs, for an xs the whole warp shares:
+// the warp's maximum of its pixels' tail starts, so that every lane's tail covers the
+// nodes from the returned index on.
+__device__ __forceinline__ int warp_tail_index(const KParamsF32& P, float xs) {
+  // order-preserving map of floats to unsigned integers, so the warp maximum is an integer one
+  const uint32_t bits = __float_as_uint(xs);
+  const uint32_t key = (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
+  const uint32_t kmax = __reduce_max_sync(__activemask(), key);
+  const float xw = __uint_as_float((kmax & 0x80000000u) ? (kmax & 0x7fffffffu) : ~kmax);
+  int lo = 0, hi = P.n_nodes;  // nodes ascend in x
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (P.gl_x_hi[mid] <= xw) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 // Fan, comet, narrow and broad band of the RRM model (number_density.py:184-342) in float32,
 // without the amplitude C.c[0] (the caller applies it).
 // The radial mask R_inner <= |X - X_0| <= R_outer and the narrow band's cut |beta| < beta_nb are

@@ -39,6 +39,27 @@ __device__ __forceinline__ float2 one_minus_emy2(float2 y) {
   return make_float2(y.x < 0.25f ? ser.x : alt.x, y.y < 0.25f ? ser.y : alt.y);
 }
 
+// One lane of one_minus_emy2, operation for operation (a packed operation rounds each lane as
+// its scalar counterpart does): band 1's inner-cutoff factor where bands 1 and 2 are not
+// evaluated but band 3, which reuses it, is.
+__device__ __forceinline__ float one_minus_emy1(float y) {
+  const float ny = -y;
+  float ser = fmaf(ny, 1.f / 720.f, 1.f / 120.f);
+  ser = fmaf(ny, ser, 1.f / 24.f);
+  ser = fmaf(ny, ser, 1.f / 6.f);
+  ser = fmaf(ny, ser, 0.5f);
+  ser = y * fmaf(ny, ser, 1.f);
+  const float alt = 1.f - ex2_ftz(-kLog2e * y);
+  return y < 0.25f ? ser : alt;
+}
+
+// (R / delta_r)^20 of a band from q = R^2 / delta_r^2, as the packed lanes form it
+__device__ __forceinline__ float band_y1(float R2, float inv_dr2) {
+  const float q = R2 * inv_dr2;
+  const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+  return q8 * q2;
+}
+
 template <int NSPEC, uint32_t FLAGS>
 __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant__ KParamsF32 P,
                                                            const double* __restrict__ u, int64_t n_pix,
@@ -70,6 +91,12 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
     const ff2 z1q = pack_ff(PS.z1[4], PS.z1[5]), z0q = pack_ff(PS.z0[4], PS.z0[5]);
     const ff2 waq = pack_ff(PS.wa[4], PS.wa[5]), wbq = pack_ff(PS.wb[4], PS.wb[5]);
     const float2 rrq = make_float2(PS.rr[4], PS.rr[5]);
+    // nodes from k12 (bands 1 and 2) and k3 (band 3) on add nothing for any pixel of the warp
+    auto tail = [&](int c) {
+      return band_zero_tail(PS.z1[c].hi, PS.z0[c].hi, PS.hs[0].hi, PS.mh[0].hi, PS.b2h, P.comp[c].c[1]);
+    };
+    const int k12 = warp_tail_index(P, fmaxf(tail(1), tail(2)));
+    const int k3 = warp_tail_index(P, tail(3));
 
     // quadrature sums per component (pairs in float2), blocks of kSumBlock nodes, Kahan across blocks
     float ps0[NSPEC], ps3[NSPEC], pS0[NSPEC], pS3[NSPEC], as0[NSPEC], ac0[NSPEC], as3[NSPEC], ac3[NSPEC];
@@ -126,8 +153,8 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
       }
 
       // ---- bands 1 and 2 (packed), number_density.py:99-110 ---------------------
-      float t4_band1;
-      {
+      float t4_band1 = 0.f;
+      if (k < k12) {
         const float2 Z = lin_ff_x2(z1b, xk, z0b);
         const float2 zz = mul2(mul2(abs2(Z), bc2(rinv)), cpair(C1, C2, 1));
         const float2 z2 = mul2(zz, zz);
@@ -146,7 +173,8 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
       }
 
       // ---- band 3 (inner-cutoff factor of band 1) -------------------------------
-      {
+      if (k < k3) {
+        if (k >= k12) t4_band1 = one_minus_emy1(band_y1(R2, C1.c[4]));
         const float Z = lin_ff(PS.z1[3], xk, PS.z0[3]);
         const float zz = fabsf(Z) * rinv * C3.c[1];
         const float z2 = zz * zz;
@@ -159,6 +187,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
           if (Fl::scat(P)) pS3[s] = fmaf(wS0[s], dens, pS3[s]);
         }
       }
+
 
       // ---- ring (.x) and feature (.y): ranges 1 and 2, number_density.py:136-181 ----
       {
