@@ -41,6 +41,11 @@ NSIDE = 512
 OBSPOS = np.array([0.7071, 0.7071, 0.0])
 OBSTIME = "2022-01-01T00:00:00"
 CPU_SAMPLE = 1 << 18
+# DRAM bytes of one launch of the headline kernel (fwd_dirbe_cp_kernel, DIRBE 25 um, HEALPix
+# nside 512, one spectral set): dram__bytes_read.sum + dram__bytes_write.sum from one ncu
+# capture of this workload (75.6 MB of unit vectors read, 119.4 MB of the 176 MB of outputs
+# written back before the kernel ended; the rest was still in L2).
+NCU_TRAFFIC_BYTES = {512: 75.6e6 + 119.4e6}
 
 
 def workload_name(nside: int) -> str:
@@ -630,7 +635,9 @@ def main():
                 "peak": (xu_peak if xu_bound else fma_peak) / 1e9,
                 "unit": "Gop/s (MUFU)" if xu_bound else "Gop/s (FP32 FMA pipe)",
                 "frac": xu_achieved / xu_peak if xu_bound else fp_achieved / fma_peak,
-                "traffic": None,
+                "traffic": NCU_TRAFFIC_BYTES.get(args.nside),
+                "traffic_source": "bytes per launch, dram__bytes_read.sum + dram__bytes_write.sum from one ncu "
+                "capture of this kernel on this workload (null for other map sizes)",
                 "peak_source": "measured in this run on this GPU: ex2.approx and fma.rn.f32 probe kernels "
                 "(zl_diag_pipe_probe); the path uses neither HBM bandwidth nor tensor cores",
                 "work": "formula-level operations per line of sight (zodipy_gb300/roofline.py): "
