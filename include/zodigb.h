@@ -282,7 +282,10 @@ ZL_API int zl_density_grid(const ZlModel* model, const double* x_dev, int32_t nx
 ZL_API int zl_mapped_pointer(const void* host_ptr, void** dev_ptr);
 
 /* Launch configuration used by zl_forward for a precision, as chosen by the
- * autotuner (threads per block, blocks per SM; 0 = library default). */
+ * autotuner (threads per block, blocks per SM in [0, 65536]; 0 = library
+ * default: one pixel per thread for the float32 forward, 8 blocks per SM for
+ * the float64 one, 96 for the adjoint).  The float32 setting also applies to
+ * zl_backward. */
 ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);
 
 /* Diagnostics (not needed by callers): 1 selects an all-float32 geometry

@@ -25,7 +25,7 @@ import torch
 from . import _lib, engine, packing
 
 TPB_CHOICES = (32, 64, 96, 128)
-BPS_CHOICES = (1, 2, 3, 4, 6, 8, 12, 16)
+BPS_CHOICES = (0, 1, 2, 3, 4, 6, 8, 12, 16, 32, 64)  # 0: the library default, one pixel per thread
 CACHE_PATH = os.environ.get("ZODIGB_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "zodigb_tune.json"))
 
 
@@ -105,7 +105,8 @@ class BatchEvaluator:
     def _key(self) -> str:
         props = torch.cuda.get_device_properties(self.u.device)
         comp = "".join(str(self.zl.comp[c].type) for c in range(self.zl.n_comps))
-        return f"{props.name}|sm{props.multi_processor_count}|p{self.prec}|c{comp}|s{self.zl.n_spec}|k{self.zl.n_nodes}"
+        return (f"v2|{props.name}|sm{props.multi_processor_count}|p{self.prec}|c{comp}|s{self.zl.n_spec}"
+                f"|k{self.zl.n_nodes}")
 
     def autotune(self, sample: int | None = 1 << 21, reps: int = 3, use_cache: bool = True):
         """Time every (threads per block, blocks per SM) on a sample; keep the fastest.
