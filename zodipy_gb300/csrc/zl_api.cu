@@ -267,6 +267,17 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
           break;
         }
       }
+    // same symmetry plane and centre as the previous component (the ring and the Earth-trailing
+    // feature): the kernels keep that component's plane projections
+    K.same_plane_prev = 0;
+    if (c > 0) {
+      const ZlComponent& Cp = m.comp[c - 1];
+      K.same_plane_prev = (Cp.sin_Omega == C.sin_Omega && Cp.cos_Omega == C.cos_Omega && Cp.sin_i == C.sin_i &&
+                           Cp.cos_i == C.cos_i && Cp.offset[0] == C.offset[0] && Cp.offset[1] == C.offset[1] &&
+                           Cp.offset[2] == C.offset[2])
+                              ? 1
+                              : 0;
+    }
     split(C.sin_Omega * C.sin_i, &K.nx, &K.nx_lo);
     split(-C.cos_Omega * C.sin_i, &K.ny, &K.ny_lo);
     split(C.cos_i, &K.nz, &K.nz_lo);

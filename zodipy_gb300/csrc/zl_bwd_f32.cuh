@@ -110,15 +110,17 @@ __device__ __forceinline__ void bwd_pixel_setup(const KParamsF32& P, const doubl
   using Fl = KFlags<FLAGS>;
   constexpr int NC = L::ncomp();
   const int nr = P.n_ranges;
-  const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+  // as the forward's pixel_setup: doubles split by bit operations, fast float-float sums
+  const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
   const PixObs O = pixel_observer(OA, i, n_pix);
-  const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
+  const ff ox = ff_split(O.ox), oy = ff_split(O.oy), oz = ff_split(O.oz);
   const uint32_t outside = O.outside;
   B.uxf = ux.hi, B.uyf = uy.hi, B.uzf = uz.hi;
   B.oxf = ox.hi, B.oyf = oy.hi, B.ozf = oz.hi;
-  const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+  const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
+  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
   const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
-  B.beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));
+  B.beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));
 #pragma unroll
   for (int r = 0; r < ZL_MAX_RANGES; ++r) {
     bool used = false;
@@ -153,32 +155,42 @@ __device__ __forceinline__ void bwd_pixel_setup(const KParamsF32& P, const doubl
     const KCompF32& C = P.comp[c];
     const int type = L::type(c);
     const ff hs = B.hs_r[L::range(c)], md = B.mid_r[L::range(c)];
-    const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
-             dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
-    const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
-    const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
-    const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
-    B.un_c[c] = un.hi + un.lo;
-    B.on_c[c] = on.hi + on.lo;
+    const bool off = Fl::offset(C, c);
+    // X_obs - X_0 (exact for the components centred on the Sun; selecting X_obs for them
+    // instead raised the forward kernel's register count past five blocks per SM)
+    const ff dx = ff_add_fast(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add_fast(oy, ff{-C.oy, -C.oy_lo}),
+             dz = ff_add_fast(oz, ff{-C.oz, -C.oz_lo});
+    if (c > 0 && ((MASK >> (c - 1)) & 1u) && C.same_plane_prev) {  // the ring's plane, for the feature
+      B.un_c[c] = B.un_c[c - 1];
+      B.on_c[c] = B.on_c[c - 1];
+    } else {
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      const ff un = ff_add_fast(ff_add_fast(ff_mul_nr(ux, nx), ff_mul_nr(uy, ny)), ff_mul_nr(uz, nz));
+      const ff on = ff_add_fast(ff_add_fast(ff_mul_nr(dx, nx), ff_mul_nr(dy, ny)), ff_mul_nr(dz, nz));
+      B.un_c[c] = un.hi + un.lo;
+      B.on_c[c] = on.hi + on.lo;
+    }
     // upstream gradient of this pixel, times (stop - start)/2: per component, or the total's
     const float hsf = hs.hi + hs.lo;
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s)
       B.gup[c][s] =
-          (float)(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) * hsf;
+          d2f_bits(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) * hsf;
     if (type == ZL_RING || type == ZL_FEATURE) {
-      const ff beta = !Fl::offset(C, c) ? B.beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
-      const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-      const ff wm = ff_add(md, beta);
-      const ff cw = ff_add(ff_add(d2, ff_neg(ff_mul(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+      const ff beta =
+          !off ? B.beta_h : ff_add_fast(ff_add_fast(ff_mul_nr(dx, ux), ff_mul_nr(dy, uy)), ff_mul_nr(dz, uz));
+      const ff d2 = !off ? r2 : ff_add_fast(ff_add_fast(ff_mul_nr(dx, dx), ff_mul_nr(dy, dy)), ff_mul_nr(dz, dz));
+      const ff wm = ff_add_fast(md, beta);
+      const ff cw = ff_add_fast(ff_add_fast(d2, ff_neg(ff_mul_nr(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
       const ff w0 = cw.hi < 0.f ? ff_sqrt(ff_neg(cw)) : ff{0.f, 0.f};
-      B.wa_c[c] = ff_add(wm, ff_neg(w0));
-      B.wb_c[c] = ff_add(wm, w0);
-      const ff res = ff_add(ff_mul(w0, w0), cw);
+      B.wa_c[c] = ff_add_fast(wm, ff_neg(w0));
+      B.wb_c[c] = ff_add_fast(wm, w0);
+      const ff res = ff_add_fast(ff_mul_nr(w0, w0), cw);
       B.rr_c[c] = res.hi + res.lo;
     }
     if (type == ZL_FEATURE) {
-      const float ex = (float)(O.ex - (double)C.ox), ey = (float)(O.ey - (double)C.oy);
+      const ff exf = ff_add_fast(ff_split(O.ex), ff{-C.ox, -C.ox_lo}), eyf = ff_add_fast(ff_split(O.ey), ff{-C.oy, -C.oy_lo});
+      const float ex = exf.hi + exf.lo, ey = eyf.hi + eyf.lo;
       const float phi = atan2f(ey, ex) + C.c[6];
       float sp, cp;
       sincosf(phi, &sp, &cp);

@@ -50,7 +50,7 @@ __host__ __device__ constexpr bool masked(int t) {
 struct KCompF32 {
   int32_t type, range, first_in_range, zero_offset;
   int32_t share_t4;  // band: index of an earlier band with the same delta_r (reuse its 1 - e^-y), else -1
-  int32_t pad_i;
+  int32_t same_plane_prev;  // 1: same symmetry plane and centre as component c - 1
   float T0, neg_delta;     // T = T_0 R^-delta of this component's range (generic layout)
   float nx, ny, nz;        // unit normal of the symmetry plane (sinO sini, -cosO sini, cosi)
   float nx_lo, ny_lo, nz_lo;  // low parts of the normal for float-float heights
@@ -172,6 +172,41 @@ __device__ __forceinline__ ff ff_from_double(double d) {
   float hi = __double2float_rn(d);
   float lo = __double2float_rn(d - (double)hi);
   return {hi, lo};
+}
+
+// ff_from_double without float64 instructions.  GB300 runs float64 (conversions included) at
+// a small fraction of its float32 rate, and each pixel's set-up splits nine doubles, so this
+// works on the bits: hi takes the top 24 significand bits (truncated), lo the next 23 (made a
+// float by setting them as the significand of 2^(E-23) and subtracting 2^(E-23) exactly);
+// 2^-47 relative, |lo| < ulp(hi).  |d| < 2^-70 (zero, subnormals) gives (+-0, 0), an absolute
+// error below 2^-70; doubles beyond the float range, inf and NaN take the conversion.
+__device__ __forceinline__ ff ff_split(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned int hw = (unsigned int)(b >> 32), lw = (unsigned int)b;
+  const int e = (int)((hw >> 20) & 0x7ffu);  // biased exponent: |d| in [2^(e-1023), 2^(e-1022))
+  const unsigned int sign = hw & 0x80000000u;
+  if (e < 1023 - 70) return {__uint_as_float(sign), 0.f};
+  if (e > 1023 + 127) return {__double2float_rn(d), 0.f};
+  const float hi = __uint_as_float(sign | ((unsigned int)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  const unsigned int base = sign | ((unsigned int)(e - 1023 - 23 + 127) << 23);  // +-2^(e-1023-23)
+  const float lo = __uint_as_float(base | ((lw & 0x1fffffffu) >> 6)) - __uint_as_float(base);
+  return {hi, lo};
+}
+
+// (float)d, rounded from the bit split (no float64 instruction)
+__device__ __forceinline__ float d2f_bits(double d) {
+  const ff s = ff_split(d);
+  return s.hi + s.lo;
+}
+
+// ff_mul without the final renormalisation: (p, e) with |e| <= ulp(p); the fast sums below
+// accept it as an operand
+__device__ __forceinline__ ff ff_mul_nr(ff a, ff b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return {p, e};
 }
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }

@@ -53,16 +53,20 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
   const int nc = L::generic ? P.n_comps : NC;
   const int nr = P.n_ranges;
-  const ff ux = ff_from_double(u[i]), uy = ff_from_double(u[n_pix + i]), uz = ff_from_double(u[2 * n_pix + i]);
+  // float-float values of the doubles by bit operations (no float64 instruction); the sums
+  // below are ff_add_fast (accurate to a few 2^-48 of their operands: the geometry needs
+  // absolute, not relative, accuracy), except where the cutoff spheres are intersected
+  const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
   const PixObs O = pixel_observer(OA, i, n_pix);
-  const ff ox = ff_from_double(O.ox), oy = ff_from_double(O.oy), oz = ff_from_double(O.oz);
+  const ff ox = ff_split(O.ox), oy = ff_split(O.oy), oz = ff_split(O.oz);
   const uint32_t outside = O.outside;
   const float uxf = ux.hi, uyf = uy.hi, uzf = uz.hi;
   const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
 
-  const ff b = ff_scale(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), 2.0f);
+  const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
+  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
   const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
-  const ff beta_h = ff_add(ff_add(ff_mul(ox, ux), ff_mul(oy, uy)), ff_mul(oz, uz));  // u . X_obs
+  const ff beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));  // u . X_obs
 
   ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
 #pragma unroll
@@ -99,6 +103,7 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   float* fx0 = S.fx0;
   float* fy1 = S.fy1;
   float* fy0 = S.fy0;
+  ff un = {0.f, 0.f}, on = {0.f, 0.f};  // u . n and (X_obs - X_0) . n of the previous component
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     if (c >= nc) break;
@@ -117,16 +122,23 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
         }
     }
     hs_c[c] = hs;
-    mh_c[c] = ff_add(md, beta_h);  // R_los + u . X_obs = hs x + mh
-    const ff dx = ff_add(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add(oy, ff{-C.oy, -C.oy_lo}),
-             dz = ff_add(oz, ff{-C.oz, -C.oz_lo});
+    mh_c[c] = ff_add_fast(md, beta_h);  // R_los + u . X_obs = hs x + mh
+    const bool off = Fl::offset(C, c);
+    // X_obs - X_0 (exact for the components centred on the Sun; selecting X_obs for them
+    // instead raised the forward kernel's register count past five blocks per SM)
+    const ff dx = ff_add_fast(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add_fast(oy, ff{-C.oy, -C.oy_lo}),
+             dz = ff_add_fast(oz, ff{-C.oz, -C.oz_lo});
     // height above the symmetry plane, linear in the node abscissa x:
     //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
-    const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
-    const ff un = ff_add(ff_add(ff_mul(ux, nx), ff_mul(uy, ny)), ff_mul(uz, nz));
-    const ff on = ff_add(ff_add(ff_mul(dx, nx), ff_mul(dy, ny)), ff_mul(dz, nz));
+    // (u . n and (X_obs - X_0) . n are kept from the previous component when it has the same
+    // plane and centre, as the ring and the Earth-trailing feature do)
+    if (!(c > 0 && C.same_plane_prev)) {
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      un = ff_add_fast(ff_add_fast(ff_mul_nr(ux, nx), ff_mul_nr(uy, ny)), ff_mul_nr(uz, nz));
+      on = ff_add_fast(ff_add_fast(ff_mul_nr(dx, nx), ff_mul_nr(dy, ny)), ff_mul_nr(dz, nz));
+    }
     z1_c[c] = ff_mul(hs, un);
-    z0_c[c] = ff_add(ff_mul(md, un), on);
+    z0_c[c] = ff_add_fast(ff_mul_nr(md, un), on);
     // |X - X_0|^2 = w^2 + b^2,  w = hs x + (mid + beta),  beta = u . (X_obs - X_0),
     // b^2 = |X_obs - X_0|^2 - beta^2;  the ring/feature use w^2 + c' with c' = b^2 - R0^2
     wm_c[c] = mh_c[c];
@@ -134,20 +146,21 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
     cw_c[c] = ff{0.f, 0.f};
     S.wa[c] = S.wb[c] = ff{0.f, 0.f};
     S.rr[c] = 0.f;
-    if (Fl::offset(C, c) || (PRECISE && ringlike(type)) || masked(type)) {
-      const ff beta = !Fl::offset(C, c) ? beta_h : ff_add(ff_add(ff_mul(dx, ux), ff_mul(dy, uy)), ff_mul(dz, uz));
-      const ff d2 = !Fl::offset(C, c) ? r2 : ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-      const ff bb = ff_add(d2, ff_neg(ff_mul(beta, beta)));
-      wm_c[c] = ff_add(md, beta);
+    if (off || (PRECISE && ringlike(type)) || masked(type)) {
+      const ff beta =
+          !off ? beta_h : ff_add_fast(ff_add_fast(ff_mul_nr(dx, ux), ff_mul_nr(dy, uy)), ff_mul_nr(dz, uz));
+      const ff d2 = !off ? r2 : ff_add_fast(ff_add_fast(ff_mul_nr(dx, dx), ff_mul_nr(dy, dy)), ff_mul_nr(dz, dz));
+      const ff bb = ff_add_fast(d2, ff_neg(ff_mul_nr(beta, beta)));
+      wm_c[c] = ff_add_fast(md, beta);
       b2_c[c] = fmaxf(bb.hi + bb.lo, 0.f);
-      cw_c[c] = masked(type) ? bb : ff_add(bb, ff_neg(ff{C.c[4], C.c[5]}));
+      cw_c[c] = masked(type) ? bb : ff_add_fast(bb, ff_neg(ff{C.c[4], C.c[5]}));
       if (ringlike(type)) {
         // R^2 - R0^2 = w^2 + c' = (w - w0)(w + w0) + (w0^2 + c'),  w0 = sqrt(max(-c', 0)):
         // each factor is linear in the node abscissa and evaluated to ~1 ulp near its zero
         const ff w0 = cw_c[c].hi < 0.f ? ff_sqrt(ff_neg(cw_c[c])) : ff{0.f, 0.f};
-        S.wa[c] = ff_add(wm_c[c], ff_neg(w0));
-        S.wb[c] = ff_add(wm_c[c], w0);
-        const ff res = ff_add(ff_mul(w0, w0), cw_c[c]);
+        S.wa[c] = ff_add_fast(wm_c[c], ff_neg(w0));
+        S.wb[c] = ff_add_fast(wm_c[c], w0);
+        const ff res = ff_add_fast(ff_mul_nr(w0, w0), cw_c[c]);
         S.rr[c] = res.hi + res.lo;
       }
     }
@@ -156,7 +169,8 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
       // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
       // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
       // two coordinates that are linear in the node abscissa
-      const float phi = atan2f((float)(O.ey - (double)C.oy), (float)(O.ex - (double)C.ox)) + C.c[6];
+      const ff ex = ff_add_fast(ff_split(O.ex), ff{-C.ox, -C.ox_lo}), ey = ff_add_fast(ff_split(O.ey), ff{-C.oy, -C.oy_lo});
+      const float phi = atan2f(ey.hi + ey.lo, ex.hi + ex.lo) + C.c[6];
       float sp, cp;
       sincosf(phi, &sp, &cp);
       const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
