@@ -176,10 +176,11 @@ __device__ __forceinline__ ff ff_from_double(double d) {
 
 // ff_from_double without float64 instructions.  GB300 runs float64 (conversions included) at
 // a small fraction of its float32 rate, and each pixel's set-up splits nine doubles, so this
-// works on the bits: hi takes the top 24 significand bits (truncated), lo the next 23 (made a
-// float by setting them as the significand of 2^(E-23) and subtracting 2^(E-23) exactly);
-// 2^-47 relative, |lo| < ulp(hi).  |d| < 2^-70 (zero, subnormals) gives (+-0, 0), an absolute
-// error below 2^-70; doubles beyond the float range, inf and NaN take the conversion.
+// works on the bits: the top 24 significand bits (truncated) and the next 23 (made a float by
+// setting them as the significand of 2^(E-23) and subtracting 2^(E-23) exactly), renormalised
+// so that hi is the rounded float value of d (as (float)d gives it); 2^-47 relative.
+// |d| < 2^-70 (zero, subnormals) gives (+-0, 0), an absolute error below 2^-70; doubles
+// beyond the float range, inf and NaN take the conversion.
 __device__ __forceinline__ ff ff_split(double d) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const unsigned int hw = (unsigned int)(b >> 32), lw = (unsigned int)b;
@@ -190,7 +191,7 @@ __device__ __forceinline__ ff ff_split(double d) {
   const float hi = __uint_as_float(sign | ((unsigned int)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
   const unsigned int base = sign | ((unsigned int)(e - 1023 - 23 + 127) << 23);  // +-2^(e-1023-23)
   const float lo = __uint_as_float(base | ((lw & 0x1fffffffu) >> 6)) - __uint_as_float(base);
-  return {hi, lo};
+  return ff_quick(hi, lo);
 }
 
 // (float)d, rounded from the bit split (no float64 instruction)

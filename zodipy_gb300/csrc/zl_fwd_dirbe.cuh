@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
       float t4_band1 = 0.f;
       if (k < k12) {
         const float2 Z = lin_ff_x2(z1b, xk, z0b);
-        const float2 zz = mul2(mul2(abs2(Z), bc2(rinv)), cpair(C1, C2, 1));
+        const float2 zz = mul2(mul2(Z, bc2(rinv)), cpair(C1, C2, 1));  // only its square is used: no |Z|
         const float2 z2 = mul2(zz, zz);
         const float2 t2 = ex2_2(mul2(bc2(-kLog2e), mul2(mul2(z2, z2), z2)));
         const float2 t3 = fma2(mul2(z2, z2), cpair(C1, C2, 2), bc2(1.f));
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
       if (k < k3) {
         if (k >= k12) t4_band1 = one_minus_emy1(band_y1(R2, C1.c[4]));
         const float Z = lin_ff(PS.z1[3], xk, PS.z0[3]);
-        const float zz = fabsf(Z) * rinv * C3.c[1];
+        const float zz = Z * rinv * C3.c[1];  // only its square is used
         const float z2 = zz * zz;
         const float t2 = ex2_ftz(-kLog2e * (z2 * z2 * z2));
         const float t3 = fmaf(z2 * z2, C3.c[2], 1.0f);
