@@ -579,7 +579,8 @@ def main():
 
     mapped = engine.mapped_pointer(u_pinned) is not None and engine.mapped_pointer(out_pinned) is not None
     e2e_mode = (
-        "zero copy: the kernel reads the pinned unit vectors and writes the pinned result (mapped host memory)"
+        "zero copy: the kernel reads the pinned unit vectors and observer record and writes the pinned result "
+        "(mapped host memory)"
         if mapped and model_mod._ZERO_COPY
         else "chunked host-to-device / device-to-host copies pipelined with the kernels"
     )

@@ -340,17 +340,21 @@ def mapped_pointer(host_tensor) -> int | None:
 
 def forward_ptr(zl_model, u_ptr: int, n: int, observers_dev, n_obs: int, precision, out_comps_ptr, out_total_ptr,
                 stream: int | None = None) -> None:
-    """``zl_forward`` on raw addresses (device buffers or mapped host memory)."""
+    """``zl_forward`` on raw addresses (device buffers or mapped host memory).  ``observers_dev``
+    is a device tensor or the integer address of the records (e.g. mapped host memory)."""
     _torch()
+    obs_ptr = observers_dev if isinstance(observers_dev, int) else observers_dev.data_ptr()
+    if stream is None:
+        stream = current_stream_handle(None if isinstance(observers_dev, int) else observers_dev.device)
     rc = _lib.load().zl_forward(
         ctypes.byref(zl_model),
         ctypes.c_void_p(u_ptr),
         int(n),
-        ctypes.c_void_p(observers_dev.data_ptr()),
+        ctypes.c_void_p(obs_ptr),
         n_obs,
         precision_code(precision),
         ctypes.c_void_p(out_comps_ptr or 0),
         ctypes.c_void_p(out_total_ptr or 0),
-        ctypes.c_void_p(stream if stream is not None else current_stream_handle(observers_dev.device)),
+        ctypes.c_void_p(stream),
     )
     _lib.check(rc, "zl_forward")

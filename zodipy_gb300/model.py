@@ -15,6 +15,8 @@ libzodigb's CUDA kernels:
 
 from __future__ import annotations
 
+import threading
+
 import numpy as np
 from scipy import integrate
 
@@ -336,9 +338,11 @@ class Model:
         if obs.shape[1] not in (1, n) or earth.shape[1] not in (1, n):
             raise ValueError("positions must be (3,) or (3, ncoords)")
         per_pixel = obs.shape[1] > 1 or earth.shape[1] > 1
+        table = None
         if not per_pixel:
             table = packing.observer_table(zl, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
-            obs_dev = engine.upload_observers(table)
+            if on_device or not _ZERO_COPY:
+                obs_dev = engine.upload_observers(table)
         if on_device:
             u_dev = unit_vectors.to(torch.float64).contiguous()
         else:
@@ -349,9 +353,10 @@ class Model:
             if not u_host.is_pinned():
                 u_host = u_host.pin_memory()
             if not per_pixel and _ZERO_COPY:
-                res = _zero_copy_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out)
+                res = _zero_copy_call(zl, u_host, table, prec, return_comps, all_spec, out)
                 if res is not None:
                     return res
+                obs_dev = engine.upload_observers(table)
             if not per_pixel and n >= 2 * _PIPE_CHUNK:
                 return _pipelined_host_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out)
             u_dev = u_host.to("cuda", non_blocking=True)
@@ -409,8 +414,31 @@ def _result_buffer(zl, n, return_comps, all_spec, out):
     return out, res_shape
 
 
-def _zero_copy_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out):
-    """One launch on mapped host memory; None when either buffer is not device-addressable."""
+_OBS_STAGING = threading.local()
+
+
+def _mapped_observers(table):
+    """The observer records in this thread's page-locked staging buffer; its device address (the
+    kernel reads the records over the host link like the unit vectors), or None if unmapped."""
+    import torch
+
+    raw = np.frombuffer(table, dtype=np.uint8)
+    dev = torch.cuda.current_device()
+    cache = getattr(_OBS_STAGING, "bufs", None)
+    if cache is None:
+        cache = _OBS_STAGING.bufs = {}
+    buf = cache.get(dev)
+    if buf is None or buf[0].numel() < raw.size:
+        t = torch.empty(max(raw.size, 4096), dtype=torch.uint8, pin_memory=True)
+        buf = cache[dev] = (t, engine.mapped_pointer(t))
+    buf[0].numpy()[: raw.size] = raw
+    return buf[1]
+
+
+def _zero_copy_call(zl, u_host, table, prec, return_comps, all_spec, out):
+    """One launch on mapped host memory (unit vectors, observer record and result); None when a
+    buffer is not device-addressable.  The staging buffer is reused only after the
+    synchronisation below, so calls of one thread never overwrite a record in use."""
     import torch
 
     host, _ = _result_buffer(zl, u_host.shape[1], return_comps, all_spec, out)
@@ -418,7 +446,10 @@ def _zero_copy_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out):
     po = engine.mapped_pointer(host) if host.is_contiguous() else None
     if pu is None or po is None:
         return None
-    engine.forward_ptr(zl, pu, u_host.shape[1], obs_dev, 1, prec, po if return_comps else None,
+    pobs = _mapped_observers(table)
+    if pobs is None:
+        return None
+    engine.forward_ptr(zl, pu, u_host.shape[1], pobs, 1, prec, po if return_comps else None,
                        None if return_comps else po)
     torch.cuda.current_stream().synchronize()
     return host if out is not None else host.numpy()
