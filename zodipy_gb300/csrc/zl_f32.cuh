@@ -159,19 +159,22 @@ __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi 
 // a quadratic whose leading coefficient a1^2 - c^2 h^2 is positive when the direction
 // itself leaves the band (|u . n| > c).  Then every node beyond the larger root is zero.
 // Returns that root for c = 2.2 dzeta (4 % inside the flush threshold, which absorbs the
-// float32 rounding of this estimate and of the node loop's zeta), -inf when the whole line
-// of sight is beyond it, +inf when no tail is guaranteed (and for NaN input).
+// float32 rounding of this estimate, its approximate divisions and square root, and the node
+// loop's zeta), -inf when the whole line of sight is beyond it, +inf when no tail is
+// guaranteed (and for NaN input).  Called by every lane of the warp together: unless every
+// pixel's direction leaves the band (A > 0), the warp has no common tail and all lanes return
+// +inf at once (random directions almost never pass this, and skip the rest).
 __device__ __forceinline__ float band_zero_tail(float a1, float a0, float h, float m, float b2h, float inv_dzeta) {
-  const float c = 2.2f / inv_dzeta;
+  const float c = __fdividef(2.2f, inv_dzeta);
   const float c2 = c * c;
   const float A = a1 * a1 - c2 * (h * h);
+  if (!__all_sync(__activemask(), A > 0.f)) return INFINITY;
   const float B = 2.f * (a1 * a0 - c2 * (h * m));
   const float C = a0 * a0 - c2 * (m * m + b2h);
-  if (!(A > 0.f)) return INFINITY;
   const float disc = B * B - 4.f * A * C;
   if (disc < 0.f) return -INFINITY;
-  const float q = -0.5f * (B + copysignf(sqrtf(disc), B));
-  const float r = fmaxf(q / A, C / q);  // the two roots; q != 0 here (disc >= 0, A > 0)
+  const float q = -0.5f * (B + copysignf(disc * rsqrt_ftz(fmaxf(disc, 1e-30f)), B));
+  const float r = fmaxf(__fdividef(q, A), __fdividef(C, q));  // the two roots (q != 0 unless B = disc = 0)
   return isnan(r) ? INFINITY : r;
 }
 
@@ -184,6 +187,7 @@ __device__ __forceinline__ int warp_tail_index(const KParamsF32& P, float xs) {
   const uint32_t key = (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
   const uint32_t kmax = __reduce_max_sync(__activemask(), key);
   const float xw = __uint_as_float((kmax & 0x80000000u) ? (kmax & 0x7fffffffu) : ~kmax);
+  if (!(xw < INFINITY)) return P.n_nodes;  // no tail (warp-uniform)
   int lo = 0, hi = P.n_nodes;  // nodes ascend in x
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
