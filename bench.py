@@ -43,9 +43,9 @@ OBSTIME = "2022-01-01T00:00:00"
 CPU_SAMPLE = 1 << 18
 # DRAM bytes of one launch of the headline kernel (fwd_dirbe_cp_kernel, DIRBE 25 um, HEALPix
 # nside 512, one spectral set): dram__bytes_read.sum + dram__bytes_write.sum from one ncu
-# capture of this workload (76.0 MB of unit vectors read, 117.4 MB of the 176 MB of outputs
+# capture of this workload (75.6 MB of unit vectors read, 117.6 MB of the 176 MB of outputs
 # written back before the kernel ended; the rest was still in L2).
-NCU_TRAFFIC_BYTES = {512: 76.0e6 + 117.4e6}
+NCU_TRAFFIC_BYTES = {512: 75.6e6 + 117.6e6}
 
 
 def workload_name(nside: int) -> str:
