@@ -168,15 +168,9 @@ __device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a,
 
 __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return {a.hi * pow2, a.lo * pow2}; }
 
-__device__ __forceinline__ ff ff_from_double(double d) {
-  float hi = __double2float_rn(d);
-  float lo = __double2float_rn(d - (double)hi);
-  return {hi, lo};
-}
-
-// ff_from_double without float64 instructions.  GB300 runs float64 (conversions included) at
-// a small fraction of its float32 rate, and each pixel's set-up splits nine doubles, so this
-// works on the bits: the top 24 significand bits (truncated) and the next 23 (made a float by
+// A double as a float-float pair, without float64 instructions.  GB300 runs float64
+// (conversions included) at a small fraction of its float32 rate, and each pixel's set-up
+// splits nine doubles, so this works on the bits: the top 24 significand bits (truncated) and the next 23 (made a float by
 // setting them as the significand of 2^(E-23) and subtracting 2^(E-23) exactly), renormalised
 // so that hi is the rounded float value of d (as (float)d gives it); 2^-47 relative.
 // |d| < 2^-70 (zero, subnormals) gives (+-0, 0), an absolute error below 2^-70; doubles
@@ -209,8 +203,6 @@ __device__ __forceinline__ ff ff_mul_nr(ff a, ff b) {
   e = fmaf(a.lo, b.hi, e);
   return {p, e};
 }
-
-__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
 // sqrt of a positive float-float (one Newton correction of the FP32 root)
 __device__ __forceinline__ ff ff_sqrt(ff a) {
