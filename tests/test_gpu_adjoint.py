@@ -273,3 +273,25 @@ def test_paired_adjoint_band_tails_healpix_order(lib, bands, per_comp):
     dev = np.abs(s_got - s_ref) / (np.abs(s_ref) + 1e-7 * np.abs(s_ref).max())
     worst = int(np.argmax(dev))
     assert dev.max() <= 1e-5, f"{names[worst]}: paired {got[worst]:.9e} scalar {ref[worst]:.9e} ({dev.max():.2e})"
+
+
+def test_adjoint_linear_in_tiny_upstream_gradient(lib):
+    """The adjoint is linear in the upstream gradient, whatever its scale: a gradient 1e-22
+    times smaller (below the range where the kernels convert doubles by bit operations) gives
+    a parameter gradient 1e-22 times smaller, not zero."""
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import engine, packing
+    from zodipy_gb300 import units as u_
+    from zodipy_gb300.healpix import pix2vec_ring
+
+    zl = zg.Model(25 * u_.micron).zl_model
+    dirs = torch.from_numpy(pix2vec_ring(16)).cuda()
+    obs = engine.upload_observers(packing.observer_table(zl, [0.9833, 0.0, 0.0], [-0.17, 0.97, 0.0], [0], any_mode=False))
+    g = 0.5 + torch.rand((1, dirs.shape[1]), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(2))
+    ref = engine.backward(zl, dirs, obs, 1, g_total=g).cpu().numpy()
+    tiny = engine.backward(zl, dirs, obs, 1, g_total=g * 1e-22).cpu().numpy()
+    big = np.abs(ref) > 1e-12 * np.abs(ref).max()
+    assert big.sum() > 10
+    np.testing.assert_allclose(tiny[big] * 1e22, ref[big], rtol=1e-5)

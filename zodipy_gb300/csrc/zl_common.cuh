@@ -188,10 +188,13 @@ __device__ __forceinline__ ff ff_split(double d) {
   return ff_quick(hi, lo);
 }
 
-// (float)d, rounded from the bit split (no float64 instruction)
+// (float)d from the bit split (no float64 instruction) where |d| is in [2^-70, 2^128); outside
+// that range (zero, tiny or huge values, inf, NaN) the conversion instruction, so that no
+// value is flushed: d here is an upstream gradient, whose scale is the caller's.
 __device__ __forceinline__ float d2f_bits(double d) {
-  const ff s = ff_split(d);
-  return s.hi + s.lo;
+  const int e = (__double2hiint(d) >> 20) & 0x7ff;
+  if (e < 1023 - 70 || e > 1023 + 127) return __double2float_rn(d);
+  return ff_split(d).hi;  // the rounded value: ff_split renormalises its pair
 }
 
 // ff_mul without the final renormalisation: (p, e) with |e| <= ulp(p); the fast sums below
