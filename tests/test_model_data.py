@@ -209,3 +209,16 @@ def test_model_set_rejects_incompatible_models(lib):
         zg.ModelSet([zg.Model(25 * u.micron), zg.Model(12 * u.micron, gauss_quad_degree=20)])
     s = zg.ModelSet([zg.Model(x * u.micron) for x in (1.25, 12, 25, 60, 100)])
     assert len(s) == 5 and [z.n_spec for z in s._zls] == [4, 1]
+
+
+@pytest.mark.parametrize("degree", [1, 2, 7, 50, 100])
+def test_quadrature_nodes_ascend(degree):
+    """The packed Gauss-Legendre nodes ascend (numpy's leggauss order, the reference's summation
+    order): the kernels' band-tail search over the node table relies on it."""
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import units as u
+
+    zl = zg.Model(25 * u.micron, gauss_quad_degree=degree).zl_model
+    x = np.array(zl.gl_x[: zl.n_nodes])
+    assert zl.n_nodes == degree
+    assert np.all(np.diff(x) > 0)
