@@ -16,6 +16,11 @@
 //
 // Built for the DIRBE layout with the built-in models' flags (cloud offset from
 // the Sun, bands with p = 4, band 3 reusing band 1's inner-cutoff term).
+//
+// Band tails: past the node from which a band's factor e^-(zeta/dzeta)^6 is zero in
+// float32 for every pixel of the warp (band_zero_tail, warp_tail_index), the band adds
+// exactly nothing, and a warp-uniform branch skips it; the maps are the same bits as
+// evaluating every node.
 #pragma once
 
 #include "zl_fwd_f32x2.cuh"
