@@ -17,7 +17,11 @@ computed here); no dataset is involved.
 
 `--impl reference` times the CPU restatement of ZodiPy's numpy path (the
 oracle, split over all host cores with a fork pool exactly like the
-reference's `nprocesses`) on a bounded sample of the same workload.
+reference's `nprocesses`) on the same whole map per step.  That arm, and the
+`cpu_baseline` leg of the GPU arm, import only numpy and `oracle/`: the model
+parameters, spectral scalars and blackbody table come from the fixtures the
+reference itself produced (tests/golden/ref_models.json, spectral.json), the
+pixel centres and Earth's position from oracle/workloads.py.
 """
 
 from __future__ import annotations
@@ -40,7 +44,6 @@ METRIC = "LOS/s DIRBE 25µm nside512: FP32 vs FP64 GPU at ≤1e-5 rel err; fwd+b
 NSIDE = 512
 OBSPOS = np.array([0.7071, 0.7071, 0.0])
 OBSTIME = "2022-01-01T00:00:00"
-CPU_SAMPLE = 1 << 18
 # DRAM bytes of one launch of the headline kernel (fwd_dirbe_cp_kernel, DIRBE 25 um, HEALPix
 # nside 512, one spectral set): dram__bytes_read.sum + dram__bytes_write.sum from one ncu
 # capture of this workload (75.6 MB of unit vectors read, 117.6 MB of the 176 MB of outputs
@@ -52,6 +55,16 @@ def workload_name(nside: int) -> str:
     """The workload both arms report (config.workload)."""
     return (f"DIRBE 25um, HEALPix nside {nside} ({12 * nside * nside} LOS), obspos (0.7071,0.7071,0) AU, GL 50, "
             "6 component maps + total")
+
+
+def bench_config(nside: int) -> dict:
+    """config of both arms' JSON lines: the same workload, stated the same way."""
+    return {
+        "workload": workload_name(nside),
+        "los_per_step": 12 * nside * nside,
+        "gauss_quad_degree": 50,
+        "l2": "GPU arm: a 256 MB buffer (> the 129 MB L2) is written before every timed step; CPU arm: n/a",
+    }
 
 
 def parse():
@@ -84,28 +97,6 @@ def build_model(precision="float32"):
     return zg.Model(25 * u.micron, name="dirbe", gauss_quad_degree=50, precision=precision)
 
 
-def oracle_desc(model):
-    from zodipy_gb300.zodiacal_light_model import COMPONENT_CUTOFFS
-
-    m = model.get_parameters()
-    sp = model._spectrum
-    return {
-        "labels": list(m["comps"]),
-        "comps": m["comps"],
-        "cutoffs": {lbl.value: COMPONENT_CUTOFFS[lbl] for lbl in model._ipd_model.comps},
-        "T_0": m["T_0"],
-        "delta": m["delta"],
-        "emissivity": sp["emissivity"],
-        "albedo": sp["albedo"],
-        "C1": sp["C1"],
-        "C2": sp["C2"],
-        "C3": sp["C3"],
-        "solar_irradiance": sp["solar_irradiance"],
-        "bb_table": model._b_nu_table,
-        "gauss_quad_degree": 50,
-    }
-
-
 def workload(nside, rank=0, world=1):
     from zodipy_gb300.ephemeris import earth_position, iso_to_mjd
     from zodipy_gb300.healpix import pix2vec_ring
@@ -116,44 +107,71 @@ def workload(nside, rank=0, world=1):
     return u, rot @ OBSPOS, earth_position(iso_to_mjd(OBSTIME))
 
 
-def cpu_sample_run(nside, n_sample, reps):
-    """Time the oracle (ZodiPy's numpy path) over all host cores; returns (LOS/s, cores, secs)."""
+def cpu_oracle_run(nside, reps):
+    """Time the oracle (ZodiPy's numpy path) on the whole map over all host cores.
+
+    Imports only numpy and oracle/: the description comes from the reference-held
+    fixtures, the inputs from oracle/workloads.py.  The fork pool is created per call,
+    as the reference's evaluate does (zodipy/model.py:182-200), so this must run before
+    the process initialises CUDA.  Returns (LOS per step, cores, seconds per step)."""
+    from oracle import workloads
     from oracle import zodi_oracle as zo
 
-    model = build_model("float64")
-    desc = oracle_desc(model)
-    u, obs, earth = workload(nside)
-    rng = np.random.default_rng(1234)
-    idx = np.sort(rng.choice(u.shape[1], size=min(n_sample, u.shape[1]), replace=False))
-    us = np.ascontiguousarray(u[:, idx])
+    desc = workloads.oracle_desc("dirbe", "dirbe_25um", 50)
+    u = workloads.healpix_ring_centres(nside)
+    earth = workloads.EARTH_2022_01_01
     cores = os.cpu_count() or 1
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        zo.evaluate_chunked(desc, us, obs, earth, nprocesses=cores)
+        zo.evaluate_chunked(desc, u, OBSPOS, earth, nprocesses=cores)
         times.append(time.perf_counter() - t0)
-    return us.shape[1], cores, times
+    return u.shape[1], cores, times
+
+
+def nvsmi_gpu_id(dev) -> str | None:
+    """The nvidia-smi identifier (UUID) of the CUDA device the bench times.
+
+    nvidia-smi numbers GPUs in its own order and ignores CUDA_VISIBLE_DEVICES, so a CUDA
+    ordinal or LOCAL_RANK can name another GPU of the machine; the UUID cannot."""
+    import torch
+
+    try:
+        uid = str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        return None
+    if not uid:
+        return None
+    uid = uid if uid.startswith("GPU-") else "GPU-" + uid
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", uid, "--query-gpu=uuid", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30)
+    except Exception:
+        return None
+    return uid if out.returncode == 0 and out.stdout.strip().lower() == uid.lower() else None
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks/throttle reasons of one GPU (by UUID), sampled every 200 ms."""
 
     Q = (
         "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
     )
 
-    def __init__(self, index):
-        self.index = index
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
         self.proc = None
         self.path = None
 
     def start(self):
+        if self.gpu_id is None:
+            return
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=open(self.path, "w"),
                 stderr=subprocess.DEVNULL,
             )
@@ -185,6 +203,7 @@ class ClockSampler:
             "sm_max_mhz": max(mx) if mx else None,
             "reasons": reasons,
             "samples": len(rows),
+            "gpu": self.gpu_id,
         }
 
 
@@ -200,7 +219,7 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    n, cores, times = cpu_sample_run(args.nside, CPU_SAMPLE, args.warmup + args.steps)
+    n, cores, times = cpu_oracle_run(args.nside, args.warmup + args.steps)
     timed = times[args.warmup :]
     t = sum(timed) / len(timed)
     v = n / t
@@ -218,19 +237,17 @@ def reference_arm(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {
-            "workload": workload_name(args.nside),
-            "implementation": "ZodiPy's numpy path (its CPU restatement), float64, all host cores",
-            "sample_los_per_step": n,
-            "l2": "n/a (CPU)",
-        },
+        "config": bench_config(args.nside),
+        "implementation": "ZodiPy's numpy path (its CPU restatement, oracle/zodi_oracle.py), float64, the "
+        "reference's fork-pool split over all host cores; parameters, spectral scalars and blackbody table "
+        "from the reference-held fixtures",
         "cpu_baseline": {
             "value": v,
             "unit": "LOS/s",
             "cores": cores,
             "kind": "port",
-            "sample": f"{n} seeded random pixels of the nside-{args.nside} map per step, numpy oracle "
-            f"(ZodiPy's per-node vectorised passes) over a {cores}-process fork pool",
+            "sample": f"the whole nside-{args.nside} map ({n} LOS) per step, numpy oracle (ZodiPy's per-node "
+            f"vectorised passes) over a {cores}-process fork pool created per step",
         },
         "e2e": {"value": v, "unit": "LOS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -390,13 +407,14 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # before any CUDA call: the oracle pool forks
-        n, cores, times = cpu_sample_run(args.nside, CPU_SAMPLE * 2, 1)
+        n, cores, times = cpu_oracle_run(args.nside, 1)
         cpu = {
             "value": n / times[0],
             "unit": "LOS/s",
             "cores": cores,
             "kind": "port",
-            "sample": f"{n} seeded random pixels of the nside-{args.nside} map, numpy oracle over a {cores}-process fork pool",
+            "sample": f"the whole nside-{args.nside} map ({n} LOS) once, numpy oracle over a {cores}-process "
+            "fork pool, parameters from the reference-held fixtures",
         }
 
     import torch
@@ -447,17 +465,26 @@ def main():
             torch.distributed.barrier()
         return [a.elapsed_time(b) for a, b in evs]
 
-    # clocks over every GPU phase of this run (float64 map, adjoint, batched, e2e), beside the
-    # samples of the headline's timed region, which at ~1.3 ms a step is shorter than the
-    # sampling interval
-    clocks_run = ClockSampler(local_rank)
+    # clocks of the timed GPU (by UUID) over every GPU phase of this run (float64 map, adjoint,
+    # batched, e2e), beside those of the headline kernel
+    gpu_id = nvsmi_gpu_id(dev)
+    clocks_run = ClockSampler(gpu_id)
     clocks_run.start()
 
     # ---- headline: float32 kernel, inputs resident ---------------------------
-    clocks = ClockSampler(local_rank)
+    # The timed region (steps x ~1.3 ms) is shorter than nvidia-smi's sampling interval, so the
+    # sampler also covers 1.5 s of back-to-back launches of the same kernel right after it.
+    clocks = ClockSampler(gpu_id)
     clocks.start()
     t32 = timed(_lib.ZL_PREC_F32, args.steps, max(args.warmup, 3))
+    soak_end = time.perf_counter() + 1.5
+    while time.perf_counter() < soak_end:
+        for _ in range(64):
+            step(_lib.ZL_PREC_F32)
+        torch.cuda.synchronize()
     clk = clocks.stop()
+    if clk is not None:
+        clk["window"] = "the timed region plus 1.5 s of back-to-back launches of the headline kernel after it"
     ms32 = sum(t32) / len(t32)
     ms_max = torch.tensor([ms32], device=dev)
     if world > 1:
@@ -488,6 +515,9 @@ def main():
         engine.forward(zl, u, obs_dev, 1, _lib.ZL_PREC_F32, want_comps=False, out_total=total, stream=sh)
         engine.backward(zl, u, obs_dev, 1, g_total=g_up, grad_out=grad, workspace=ws, stream=sh)
 
+    def fwd_only():  # the forward of fwd_bwd, alone: total map only, as the loss needs
+        engine.forward(zl, u, obs_dev, 1, _lib.ZL_PREC_F32, want_comps=False, out_total=total, stream=sh)
+
     def bwd_only():
         engine.backward(zl, u, obs_dev, 1, g_total=g_up, grad_out=grad, workspace=ws, stream=sh)
 
@@ -506,8 +536,9 @@ def main():
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in ts) / k
 
-    fb_ms = timed_fn(fwd_bwd, max(2, min(args.steps, 5)), 2)
-    bwd_ms = timed_fn(bwd_only, max(2, min(args.steps, 5)), 1)
+    fb_ms = timed_fn(fwd_bwd, max(3, min(args.steps, 10)), 2)
+    fwd_tot_ms = timed_fn(fwd_only, max(3, min(args.steps, 10)), 1)
+    bwd_ms = timed_fn(bwd_only, max(3, min(args.steps, 10)), 1)
 
     # ---- batched observers: 256 observers, uneven counts, one graph launch -----
     batched = None
@@ -536,6 +567,14 @@ def main():
             torch.cuda.synchronize()
             bt.append(a.elapsed_time(b))
         bms = sum(bt) / len(bt)
+        # the whole batch in float64 (plain kernel, same inputs): the float32 error of every LOS
+        _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, 0), "reset launch")
+        ev64 = BatchEvaluator(pm.zl_model, bu, bobs, bcounts, workload(args.nside)[2], precision="float64")
+        t64b = ev64.run()
+        rel_b = ((ev.total - t64b).abs() / t64b.abs()).flatten()
+        err_b = {"max": float(rel_b.max()), "median": float(rel_b.median()), "values": int(rel_b.numel()),
+                 "against": "the float64 plain kernel on the same batch"}
+        del ev64, t64b, rel_b
         batched = {
             "workload": "planck18 857 GHz, 256 observers on a 1 AU circle (z ~ N(0, 0.01) AU), "
             f"pixel counts U{{10000..500000}} (seed 2024): {nb} LOS, GL 50, float32, one CUDA-graph launch",
@@ -543,6 +582,7 @@ def main():
             "ms_per_launch": bms,
             "los_per_s": nb / (bms * 1e-3),
             "autotuned_launch": {"threads_per_block": tpb, "blocks_per_sm": bps_b},
+            "rel_err_fp32_vs_fp64": err_b,
         }
         del ev, bu
         _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, 0), "reset launch")
@@ -622,19 +662,19 @@ def main():
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {
-                "workload": workload_name(args.nside),
-                "implementation": "libzodigb float32-bulk kernel (float-float where needed), one GPU",
-                "l2": "flushed (256 MB write) before every timed step",
-                "parallelism": f"replicas x{world}, no collective on the data path",
-            },
+            "config": bench_config(args.nside),
+            "implementation": "libzodigb float32-bulk kernel (float-float where needed), one GPU per rank",
+            "parallelism": f"replicas x{world}, no collective on the data path",
             "fp64_los_per_s": n / (ms64 * 1e-3),
             "fp64_ms_per_step": ms64,
             "speedup_fp32_vs_fp64": ms64 / ms32,
             "rel_err_fp32_vs_fp64": err,
             "fwd_bwd_ms": fb_ms,
+            "fwd_ms": fwd_tot_ms,
             "bwd_ms": bwd_ms,
-            "fwd_bwd_over_fwd": fb_ms / ms32,
+            # like with like: the forward inside fwd_bwd (total map only) timed alone
+            "fwd_bwd_over_fwd": fb_ms / fwd_tot_ms,
+            "fwd_bwd_over_headline_fwd": fb_ms / ms32,
             "n_params": int(grad.numel()),
             "batched": batched,
             "roofline": {

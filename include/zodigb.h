@@ -221,7 +221,10 @@ ZL_API int zl_backward(const ZlModel* model, const double* unit_vectors_dev, int
  * loads it until exit.  Returns ZL_ERR_SPACE when zl_backward_workspace_bytes()
  * exceeds 32 MiB (single-band DIRBE: up to 3.4 million pixels).  Calls that
  * overlap on the GPU share the array and race: serialise them.  The first call
- * on a device looks up the array's address; make it before any stream capture. */
+ * on a device looks up the array's address; make it before any stream capture.
+ * That address is kept for the life of the process: after cudaDeviceReset() (or
+ * anything else that destroys the device's primary context) it no longer holds,
+ * so a process that resets a device must not call zl_backward_static again. */
 ZL_API int zl_backward_static(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
                               const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
                               const double* g_total_dev, double* grad_out_dev, void* stream);
@@ -312,6 +315,13 @@ ZL_API int zl_diag_pipe_probe(int32_t which, int32_t iters, float* sink_dev, int
  * per-node angle of the feature and of scattering), n device floats each, on
  * `stream`.  For checking it against a reference atan2. */
 ZL_API int zl_diag_atan2(const float* y_dev, const float* x_dev, float* out_dev, int64_t n, void* stream);
+
+/* Diagnostics: the kernels' conversion of doubles without float64 instructions.  For
+ * each of n device doubles d[i], out[3i], out[3i+1] receive the float-float pair (hi, lo)
+ * the kernels split d[i] into and out[3i+2] the float value they round d[i] to (an
+ * upstream gradient's conversion); out holds 3n device floats.  For checking them
+ * against the conversion instruction. */
+ZL_API int zl_diag_d2f(const double* d_dev, float* out_dev, int64_t n, void* stream);
 
 #ifdef __cplusplus
 }

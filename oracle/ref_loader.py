@@ -24,7 +24,13 @@ import types
 
 import numpy as np
 
-DEFAULT_REF_ROOT = os.environ.get("ZODIPY_REF_ROOT", "/root/reference")
+# Root of a ZodiPy v1.1.3 source tree (the directory holding ``zodipy/``); there is no built-in
+# default: set ZODIPY_REF_ROOT or pass the path.
+REF_ROOT_ENV = "ZODIPY_REF_ROOT"
+
+
+def ref_root_from_env() -> str | None:
+    return os.environ.get(REF_ROOT_ENV) or None
 
 # (1 MJy / AU) in Jy / cm, the unit change astropy applies to the RRM calibration
 # (unpack_model.py:131-132): 1e6 Jy over 1 au = 1.495978707e13 cm (IAU 2012 exact).
@@ -115,11 +121,15 @@ def _install_astropy_stub() -> None:
     )
 
 
-def load_reference(ref_root: str = DEFAULT_REF_ROOT) -> types.SimpleNamespace:
+def load_reference(ref_root: str | None = None) -> types.SimpleNamespace:
     """Execute the reference's numeric modules in place and return them.
 
-    Raises FileNotFoundError when the reference tree is absent (the GPU machine).
+    ``ref_root`` defaults to $ZODIPY_REF_ROOT.  Raises FileNotFoundError when
+    neither names a ZodiPy source tree.
     """
+    ref_root = ref_root or ref_root_from_env()
+    if not ref_root:
+        raise FileNotFoundError(f"no reference tree: pass its path or set {REF_ROOT_ENV}")
     pkg_dir = os.path.join(ref_root, "zodipy")
     if not os.path.isdir(pkg_dir):
         raise FileNotFoundError(f"reference package not found at {pkg_dir}")
@@ -146,8 +156,9 @@ def load_reference(ref_root: str = DEFAULT_REF_ROOT) -> types.SimpleNamespace:
     return types.SimpleNamespace(**mods)
 
 
-def reference_available(ref_root: str = DEFAULT_REF_ROOT) -> bool:
-    return os.path.isdir(os.path.join(ref_root, "zodipy"))
+def reference_available(ref_root: str | None = None) -> bool:
+    ref_root = ref_root or ref_root_from_env()
+    return bool(ref_root) and os.path.isdir(os.path.join(ref_root, "zodipy"))
 
 
 class _V:

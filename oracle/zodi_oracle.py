@@ -419,11 +419,12 @@ def grid_number_density(desc: dict, x, y, z, earth_xyz) -> np.ndarray:
     return out
 
 
-def evaluate_chunked(desc, unit_vectors, obs_xyz, earth_xyz, nprocesses=1, fix_b0=False):
+def evaluate_chunked(desc, unit_vectors, obs_xyz, earth_xyz, nprocesses=1, fix_b0=False, start_method="fork"):
     """``evaluate`` split over coordinate chunks like ``model.py:182-200``.
 
-    The pool is created with the fork start method exactly like the reference;
-    callers that have initialised CUDA must not use ``nprocesses > 1``.
+    By default the pool is created with the fork start method exactly like the
+    reference; a process that has initialised CUDA must pass
+    ``start_method="spawn"`` (a pool forked after CUDA initialisation can hang).
     """
     u = np.asarray(unit_vectors, dtype=np.float64)
     n = u.shape[-1]
@@ -435,7 +436,7 @@ def evaluate_chunked(desc, unit_vectors, obs_xyz, earth_xyz, nprocesses=1, fix_b
     per_pixel_obs = obs.ndim > 1 and obs.shape[-1] == n and n > 1
     u_splits = np.array_split(u, nprocesses, axis=-1)
     o_splits = np.array_split(obs, nprocesses, axis=-1) if per_pixel_obs else [obs] * nprocesses
-    with multiprocessing.get_context("fork").Pool(nprocesses) as pool:
+    with multiprocessing.get_context(start_method).Pool(nprocesses) as pool:
         parts = [
             pool.apply_async(evaluate, (desc, us, os_, earth_xyz, fix_b0)) for us, os_ in zip(u_splits, o_splits)
         ]

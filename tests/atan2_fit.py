@@ -1,4 +1,4 @@
-"""Fit of the polynomial in atan2_poly (zl_common.cuh).
+"""Fit of the polynomial in atan2_poly (zodipy_gb300/csrc/zl_common.cuh).
 
 atan t = t + t^3 Q(t^2) on t in [0, 1]; Q of degree 7 minimises the maximum relative
 error of atan by iteratively reweighted least squares (Lawson's method) on
@@ -6,7 +6,10 @@ Chebyshev-distributed points.  Prints the coefficients (low order first) as floa
 literals and the float32-evaluated error of atan on [0, 1] and of the octant-reduced
 atan2 on random points (FMA emulated in float64, the reciprocal correctly rounded).
 
-    python zodipy_gb300/csrc/fit_atan2_poly.py
+    python tests/atan2_fit.py
+
+tests/test_atan2_fit.py re-derives the coefficients with this fit and checks them
+against the ones compiled into the kernels.
 """
 
 import numpy as np

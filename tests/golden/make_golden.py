@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run in a checkout where the ZodiPy v1.1.3 source tree is available (default
-/root/reference, override with ZODIPY_REF_ROOT):
+Run with the path of a ZodiPy v1.1.3 source tree (the directory that holds
+``zodipy/``), given as ``--ref PATH`` or in $ZODIPY_REF_ROOT:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --ref PATH [grid | rrm | configs]
 
 The reference's own numeric modules are executed in place under an astropy
 stand-in (oracle/ref_loader.py).  Inputs that the reference would get from
@@ -18,8 +18,9 @@ those inputs to the per-component emission.  Outputs:
                       points (tests/dirbe_tabulated.py of the reference)
   grid_<case>.npz     inputs + reference grid_number_density output
 
-``python tests/golden/make_golden.py grid`` regenerates only the grid fixtures,
-``... rrm`` only ref_models.json and the RRM fixtures.
+``... grid`` regenerates only the grid fixtures, ``... rrm`` only
+ref_models.json and the RRM fixtures, ``... configs`` only the fixtures on the
+benchmark configurations' inputs (los_cfg*.npz).
 """
 
 from __future__ import annotations
@@ -37,7 +38,7 @@ sys.path.insert(0, REPO)
 
 from oracle import zodi_oracle  # noqa: E402
 from oracle.ref_loader import (  # noqa: E402
-    DEFAULT_REF_ROOT,
+    REF_ROOT_ENV,
     load_reference,
     reference_evaluate,
     reference_fd_gradient,
@@ -227,12 +228,68 @@ def make_rrm(ref) -> None:
         nd.get_earthpos_inst = saved
 
 
+def make_config_cases(ref) -> None:
+    """The reference on seeded subsets of each benchmark configuration's own inputs
+    (``los_cfg*.npz``): the map, observers, spectral set and degree of the five configs,
+    at a size the reference runs in seconds.  The GPU tests compare the full-size runs with
+    the oracle, and these fixtures pin the oracle to the reference on the same geometry."""
+    from zodipy_gb300.batch import uneven_observers
+
+    rng = np.random.default_rng(20260101)
+    earth_2022 = earth_position(iso_to_mjd("2022-01-01T00:00:00"))
+    lam = np.linspace(80, 130, 64)
+    w_bp = np.exp(-0.5 * ((lam - 100) / 10) ** 2)
+
+    def healpix_subset(nside, n):
+        idx = np.sort(rng.choice(12 * nside * nside, n, replace=False))
+        return pix2vec_ring(nside, idx)
+
+    # config 3: per-pixel observers of the first four batch observers (one map of directions each)
+    bobs, _ = uneven_observers(256, seed=2024)
+    n3 = 96
+    u3 = random_sphere(4 * n3, seed=2025)
+    obs3 = np.repeat(bobs[:, :4], n3, axis=1)
+    # config 5: three observers at 0/120/240 deg on the 1 AU circle, nside 2048
+    ang = np.radians([0.0, 120.0, 240.0])
+    n5 = 128
+    u5 = healpix_subset(2048, 3 * n5)
+    obs5 = np.repeat(np.stack([np.cos(ang), np.sin(ang), np.zeros(3)]), n5, axis=1)
+    cases = {
+        "cfg1_dirbe25_nside128": ("dirbe", 25.0, "micron", None, healpix_subset(128, 1024), [0.9833, 0.0, 0.0], 50),
+        "cfg2_bandpass_nside512": ("dirbe", lam, "micron", w_bp, healpix_subset(512, 1024), [0.7071, 0.7071, 0.0], 50),
+        "cfg3_planck18_batch": ("planck18", 857.0, "GHz", None, u3, obs3, 50),
+        "cfg4_dirbe12_nside256": ("dirbe", 12.0, "micron", None, healpix_subset(256, 1024), [0.9833, 0.0, 0.0], 50),
+        "cfg5_dirbe60_gl100": ("dirbe", 60.0, "micron", None, u5, obs5, 100),
+    }
+    for key, (name, x, unit, w, u, obs, deg) in cases.items():
+        payload = make_case(ref, name, x, unit, w, u, np.asarray(obs, dtype=np.float64), earth_2022, deg)
+        np.savez_compressed(os.path.join(HERE, f"los_{key}.npz"), **payload)
+
+
+def parse_args(argv):
+    """(reference root, remaining words): ``--ref PATH`` wins over $ZODIPY_REF_ROOT."""
+    argv = list(argv)
+    ref_root = os.environ.get(REF_ROOT_ENV)
+    if "--ref" in argv:
+        i = argv.index("--ref")
+        ref_root = argv[i + 1]
+        del argv[i : i + 2]
+    if not ref_root:
+        raise SystemExit(f"usage: make_golden.py --ref PATH [grid|rrm]  (or set {REF_ROOT_ENV})")
+    return ref_root, argv
+
+
 def main() -> None:
-    ref_root = os.environ.get("ZODIPY_REF_ROOT", DEFAULT_REF_ROOT)
+    ref_root, words = parse_args(sys.argv[1:])
     ref = load_reference(ref_root)
+    sys.argv[1:] = words
     if sys.argv[1:] == ["grid"]:
         make_grids(ref)
         print("wrote grid fixtures to", HERE)
+        return
+    if sys.argv[1:] == ["configs"]:
+        make_config_cases(ref)
+        print("wrote benchmark-configuration fixtures to", HERE)
         return
     if sys.argv[1:] == ["rrm"]:
         with open(os.path.join(HERE, "ref_models.json"), "w") as f:
@@ -242,6 +299,7 @@ def main() -> None:
         return
     make_grids(ref)
     make_rrm(ref)
+    make_config_cases(ref)
     models = dump_models(ref)
     with open(os.path.join(HERE, "ref_models.json"), "w") as f:
         json.dump(models, f, indent=1)

@@ -38,8 +38,27 @@ def test_reference_arm_prints_one_contract_line():
     sys.path.insert(0, REPO)
     import bench
 
-    assert d["config"]["workload"] == bench.workload_name(64)
+    assert d["config"] == bench.bench_config(64)  # the GPU arm reports the same config
+    assert d["config"]["los_per_step"] == 12 * 64 * 64
     assert d["metric"] == bench.METRIC
+
+
+def test_reference_arm_does_not_touch_the_package():
+    """The reference arm runs the oracle on reference-held data: after it, no module of the
+    package is imported and the package's shared library is not mapped."""
+    code = (
+        "import runpy, sys\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', '--nside', '16']\n"
+        "runpy.run_path('bench.py', run_name='__main__')\n"
+        "mods = sorted(m for m in sys.modules if m.startswith('zodipy_gb300'))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert not mods, mods\n"
+        "assert 'libzodigb' not in maps\n"
+        "print('clean')\n"
+    )
+    r = subprocess.run([sys.executable, "-c", code], cwd=REPO, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().splitlines()[-1] == "clean"
 
 
 def test_reference_arm_runs_on_rank_zero_only():

@@ -170,9 +170,13 @@ __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return {a.hi * pow2, 
 
 // A double as a float-float pair, without float64 instructions.  GB300 runs float64
 // (conversions included) at a small fraction of its float32 rate, and each pixel's set-up
-// splits nine doubles, so this works on the bits: the top 24 significand bits (truncated) and the next 23 (made a float by
-// setting them as the significand of 2^(E-23) and subtracting 2^(E-23) exactly), renormalised
-// so that hi is the rounded float value of d (as (float)d gives it); 2^-47 relative.
+// splits nine doubles, so this works on the bits: the top 24 significand bits (truncated) and
+// the next 23 (made a float by setting them as the significand of 2^(E-23) and subtracting
+// 2^(E-23) exactly), renormalised so that hi is the rounded float value of d (as (float)d
+// gives it); 2^-47 relative.  The 6 significand bits below those 47 are not kept, but they
+// stick to the lowest kept bit (set it when any of them is set), so that a value just above a
+// halfway point between two floats still rounds up when the pair is renormalised, as
+// round-to-nearest of the double does; an exact halfway point rounds to even in both.
 // |d| < 2^-70 (zero, subnormals) gives (+-0, 0), an absolute error below 2^-70; doubles
 // beyond the float range, inf and NaN take the conversion.
 __device__ __forceinline__ ff ff_split(double d) {
@@ -184,7 +188,8 @@ __device__ __forceinline__ ff ff_split(double d) {
   if (e > 1023 + 127) return {__double2float_rn(d), 0.f};
   const float hi = __uint_as_float(sign | ((unsigned int)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
   const unsigned int base = sign | ((unsigned int)(e - 1023 - 23 + 127) << 23);  // +-2^(e-1023-23)
-  const float lo = __uint_as_float(base | ((lw & 0x1fffffffu) >> 6)) - __uint_as_float(base);
+  const unsigned int low23 = ((lw & 0x1fffffffu) >> 6) | ((lw & 0x3fu) != 0u ? 1u : 0u);  // sticky
+  const float lo = __uint_as_float(base | low23) - __uint_as_float(base);
   return ff_quick(hi, lo);
 }
 
@@ -253,7 +258,7 @@ __device__ __forceinline__ float rcp_ftz(float x) {
 // t = min(|x|, |y|) / max(|x|, |y|) in [0, 1] (one rcp.approx), atan t = t + t^3 Q(t^2)
 // with Q of degree 7, its coefficients fitted for this library by iteratively reweighted
 // least squares (Lawson's method) on the relative error of atan over [0, 1] (1.1 ulp
-// there in float32; fit_atan2_poly.py beside this file reproduces them); then atan2 = pi/2 - atan t where |y| > |x|, pi - (that) where
+// there in float32; tests/atan2_fit.py reproduces them); then atan2 = pi/2 - atan t where |y| > |x|, pi - (that) where
 // x < 0, and the sign of y.  About 3 ulp from the correctly rounded atan2 for finite
 // arguments; (0, 0) gives 0.
 __device__ __forceinline__ float atan2_poly(float y, float x) {

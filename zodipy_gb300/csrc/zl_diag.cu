@@ -70,7 +70,24 @@ __global__ void atan2_eval(const float* __restrict__ y, const float* __restrict_
     out[i] = zl::atan2_poly(y[i], x[i]);
 }
 
+__global__ void d2f_eval(const double* __restrict__ d, float* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const zl::ff p = zl::ff_split(d[i]);
+    out[3 * i] = p.hi;
+    out[3 * i + 1] = p.lo;
+    out[3 * i + 2] = zl::d2f_bits(d[i]);
+  }
+}
+
 }  // namespace
+
+extern "C" ZL_API int zl_diag_d2f(const double* d_dev, float* out_dev, int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && (!d_dev || !out_dev))) return ZL_ERR_ARG;
+  if (n == 0) return ZL_OK;
+  const int64_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  d2f_eval<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(d_dev, out_dev, n);
+  return cudaGetLastError() == cudaSuccess ? ZL_OK : ZL_ERR_CUDA;
+}
 
 extern "C" ZL_API int zl_diag_atan2(const float* y_dev, const float* x_dev, float* out_dev, int64_t n, void* stream) {
   if (n < 0 || (n > 0 && (!y_dev || !x_dev || !out_dev))) return ZL_ERR_ARG;

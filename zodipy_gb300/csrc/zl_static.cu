@@ -20,8 +20,11 @@
 // host threads) race on it; serialise them.  The first call on each device
 // looks up the array's device address with cudaGetSymbolAddress (once per
 // device, with that device current); make that first call before any stream
-// capture.  The entry point itself calls no allocating CUDA or library
-// routine.
+// capture.  The looked-up address is cached per device for the life of the
+// process; cudaDeviceReset() (or any destruction of the primary context) unloads
+// the module that holds the array, so after a reset the cached address is stale
+// and zl_backward_static must not be called again in that process.  The entry
+// point itself calls no allocating CUDA or library routine.
 #include <mutex>
 
 #include "zl_common.cuh"
