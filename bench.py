@@ -552,7 +552,7 @@ def main():
         nb = int(bcounts.sum())
         bu = random_directions_device(nb, seed=2025, device=dev)
         ev = BatchEvaluator(pm.zl_model, bu, bobs, bcounts, workload(args.nside)[2], precision="float32")
-        tpb, bps_b, _ = ev.autotune(sample=1 << 21, reps=2, use_cache=False)
+        tpb, bps_b, tile_b, _ = ev.autotune(sample=1 << 21, reps=2, use_cache=False)
         ev.capture()
         for _ in range(2):
             ev.replay()
@@ -568,7 +568,6 @@ def main():
             bt.append(a.elapsed_time(b))
         bms = sum(bt) / len(bt)
         # the whole batch in float64 (plain kernel, same inputs): the float32 error of every LOS
-        _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, 0), "reset launch")
         ev64 = BatchEvaluator(pm.zl_model, bu, bobs, bcounts, workload(args.nside)[2], precision="float64")
         t64b = ev64.run()
         rel_b = ((ev.total - t64b).abs() / t64b.abs()).flatten()
@@ -581,11 +580,11 @@ def main():
             "los": nb,
             "ms_per_launch": bms,
             "los_per_s": nb / (bms * 1e-3),
-            "autotuned_launch": {"threads_per_block": tpb, "blocks_per_sm": bps_b},
+            "autotuned_launch": {"threads_per_block": tpb, "blocks_per_sm": bps_b, "queue_tile": tile_b,
+                                 "sorted_by_latitude": ev.sorted, "band_tails": ev.sorted},
             "rel_err_fp32_vs_fp64": err_b,
         }
         del ev, bu
-        _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, 0), "reset launch")
 
     # ---- XU roofline --------------------------------------------------------
     sink = torch.empty(8 * 1024, dtype=torch.float32, device=dev)

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define ZL_ABI_VERSION 2
+#define ZL_ABI_VERSION 3
 
 #define ZL_MAX_COMPS 8   /* components per model (DIRBE has 6) */
 #define ZL_MAX_RANGES 8  /* distinct (inner, outer) cutoff pairs per model */
@@ -137,6 +137,45 @@ typedef struct ZlObserver {
   uint32_t reserved;
 } ZlObserver;
 
+/* Which float32 kernel serves a call (ZlLaunch.kernel). */
+enum {
+  ZL_KERNEL_AUTO = 0,          /* the fastest measured kernel for the model's layout */
+  ZL_KERNEL_ONE_PIXEL = 1,     /* one pixel per thread, components in order (forward and adjoint) */
+  ZL_KERNEL_TWO_PIXEL = 2,     /* forward: two pixels per thread on packed float32 (built-in layouts) */
+  ZL_KERNEL_PLAIN_GEOMETRY = 3 /* forward, DIRBE layout: all-float32 geometry (a precision study) */
+};
+
+/* Launch options of one call (NULL = the defaults).  The library keeps no launch
+ * state between calls: each call's options apply to that call only, so callers
+ * with different options (an autotuner, another model) never affect each other.
+ *
+ * Work queue: with tile > 0 the forward's blocks pull tiles of `tile` items (pixels;
+ * pixel pairs for the two-pixel kernel) from the counter queue_dev[0] until the
+ * work runs out, instead of a fixed block-to-tile assignment.  queue_dev is two
+ * uint32 words of device memory owned by the caller, zero before the first call;
+ * each call leaves them zero again (the last block to finish resets them), so a
+ * call can be replayed from a CUDA graph.  Calls that share a queue must not
+ * overlap on the GPU.  No block waits for another.
+ *
+ * out_index_dev: pixel i's outputs go to column out_index_dev[i] (a permutation of
+ * 0 .. n_pix-1) instead of column i; lets a caller evaluate its pixels in another
+ * order (for example sorted by latitude, so that a warp's lines of sight are alike)
+ * and still receive them in its own layout. */
+typedef struct ZlLaunch {
+  int32_t threads_per_block; /* 32 .. 128, a multiple of 32; 0 = 128 */
+  int32_t blocks_per_sm;     /* cap of the grid in blocks per SM, 0 .. 65536; 0 = the default of the
+                                entry point (float32 forward: one block per tile; float64 forward: 8;
+                                adjoint: 96) */
+  int32_t kernel;            /* ZL_KERNEL_* */
+  int32_t band_tails;        /* two-pixel kernel: 1 = skip the bands' zero tails (coherent inputs:
+                                a HEALPix ring, directions sorted by latitude), 0 = evaluate every
+                                node (the default; no effect on the results, only on speed) */
+  int32_t tile;              /* > 0: work-queue tile in items, a multiple of threads_per_block; 0 = no queue */
+  int32_t reserved;
+  uint32_t* queue_dev;       /* tile > 0: the queue's two words (see above) */
+  const int64_t* out_index_dev; /* NULL or n_pix output columns */
+} ZlLaunch;
+
 /* Version of the library (== ZL_ABI_VERSION of the build). */
 ZL_API int zl_abi_version(void);
 
@@ -165,6 +204,13 @@ ZL_API int zl_forward(const ZlModel* model, const double* unit_vectors_dev, int6
                const ZlObserver* observers_dev, int32_t n_obs, int32_t precision,
                double* out_comps_dev, double* out_total_dev, void* stream);
 
+/* zl_forward with launch options (NULL = zl_forward).  Forward entry point for
+ * autotuners and batched callers: launch shape, kernel choice, work queue and
+ * output permutation per call (ZlLaunch). */
+ZL_API int zl_forward_ex(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+                         const ZlObserver* observers_dev, int32_t n_obs, int32_t precision, double* out_comps_dev,
+                         double* out_total_dev, const ZlLaunch* launch, void* stream);
+
 /* Forward pass for time-ordered data: one observer and one Earth position per
  * pixel (zodipy/model.py:119-203 with obstime.size == n_pix and obspos of shape
  * (3, n_pix)).  Replaces the same loop as zl_forward; the cutoff rule of
@@ -192,8 +238,18 @@ ZL_API int zl_forward_tod(const ZlModel* model, const double* unit_vectors_dev, 
  *   d/d T_0, d/d delta
  *   per spectral set s: d/d emissivity[c] (c = 0..n_comps-1), d/d albedo[c],
  *     d/d C1, C2, C3, d/d solar_irradiance (the interpolated scalars)
- * Supported for ZL_KELSALL models (any mix of the four Kelsall types); a
- * ZL_RRM model is refused with ZL_ERR_MODEL.  The sum over pixels is deterministic:
+ * for ZL_KELSALL models with the built-in component layouts (cloud, 3 bands[, ring,
+ * feature]), and for ZL_RRM models (zodipy/zodiacal_light_model.py:90-102):
+ *   per component c, in model order: d/d x_0, y_0, z_0, i [deg], Omega [deg], then
+ *     the type's own parameters in ZlComponent order (fan: gamma, Z_0, Q, P, R_outer |
+ *     comet: gamma, Z_0, P, amp, R_inner, R_outer | narrow band: gamma, A, G, R_inner,
+ *     R_outer, beta_nb [deg] | broad band: gamma, A, R_inner, R_outer, beta_bb [deg],
+ *     sigma_bb [deg] | interstellar: amp | ring: n_0, R, sigma_r, sigma_z, A |
+ *     feature: n_0, R, sigma_r, sigma_z, theta [deg], sigma_theta [deg], A)
+ *   d/d T_0 of every component, then d/d delta of every component
+ *   d/d calibration of every spectral set
+ * (a mask edge -- R_inner, R_outer, beta_nb where it cuts -- contributes nothing: the
+ * quadrature's nodes do not move with it).  The sum over pixels is deterministic:
  * fixed 128-pixel tiles reduced in a fixed order, independent of the launch. */
 
 /* Number of entries of the gradient vector for this model. */
@@ -212,6 +268,14 @@ ZL_API int zl_backward(const ZlModel* model, const double* unit_vectors_dev, int
                        const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
                        const double* g_total_dev, double* grad_out_dev, void* workspace_dev,
                        size_t workspace_bytes, void* stream);
+
+/* zl_backward with launch options (NULL = zl_backward): blocks_per_sm and kernel
+ * (ZL_KERNEL_AUTO or ZL_KERNEL_ONE_PIXEL) apply; the adjoint's 128-pixel tiles are
+ * fixed, and the gradient does not depend on the options (same bits). */
+ZL_API int zl_backward_ex(const ZlModel* model, const double* unit_vectors_dev, int64_t n_pix,
+                          const ZlObserver* observers_dev, int32_t n_obs, const double* g_comps_dev,
+                          const double* g_total_dev, double* grad_out_dev, void* workspace_dev, size_t workspace_bytes,
+                          const ZlLaunch* launch, void* stream);
 
 /* Backward pass without a caller-allocated workspace, for callers that cannot
  * allocate device memory (a host that owns all device memory through its own
@@ -283,26 +347,6 @@ ZL_API int zl_density_grid(const ZlModel* model, const double* x_dev, int32_t nx
  * memory directly: pass the returned pointers to zl_forward instead of device
  * buffers.  Returns ZL_ERR_CUDA when the memory is not mapped. */
 ZL_API int zl_mapped_pointer(const void* host_ptr, void** dev_ptr);
-
-/* Launch configuration used by zl_forward for a precision, as chosen by the
- * autotuner (threads per block, blocks per SM in [0, 65536]; 0 = library
- * default: one pixel per thread for the float32 forward, 8 blocks per SM for
- * the float64 one, 96 for the adjoint).  The float32 setting also applies to
- * zl_backward. */
-ZL_API int zl_set_launch(int32_t precision, int32_t threads_per_block, int32_t blocks_per_sm);
-
-/* Diagnostics (not needed by callers): 1 selects an all-float32 geometry
- * variant of the DIRBE-layout float32 kernel, used to measure what the
- * float-float ring/feature geometry buys.  Applies to later zl_forward calls
- * of every thread. */
-ZL_API int zl_debug_plain_geometry(int32_t on);
-
-/* Diagnostics: 1 keeps the one-pixel float32 kernel for the built-in layouts
- * where zl_forward otherwise integrates two pixels per thread with packed
- * float32 instructions (the Planck layout); -1 selects the two-pixel kernel
- * for the DIRBE layout as well; 0 restores the default.  For comparing the
- * kernels; applies to later calls of every thread. */
-ZL_API int zl_debug_one_pixel(int32_t on);
 
 /* Diagnostics: launch a pipe-throughput probe on `stream` (which = 0: MUFU
  * ex2, which = 1: FP32 FMA, which = 2: packed FP32 FMA counted per FMA), `iters` iterations of 8 independent chains per

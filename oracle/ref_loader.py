@@ -366,3 +366,51 @@ def reference_fd_gradient(ref, model_name, u, obs, earth, bb_table, x_model, wei
         names.append(key)
         grads.append((vals[0] - vals[1]) / (2 * h))
     return names, np.asarray(grads), L0
+
+
+def reference_fd_gradient_rrm(ref, model_name, u, obs, earth, bb_table, x_model, weights, degree, a,
+                              rel_step=1e-5):
+    """Central finite differences of L = sum_i a_i total_i through the reference's own code, for
+    the Rowan-Robinson & May model (``brightness.py:59-83``, ``number_density.py:184-404``).
+
+    Parameters: every component's init parameters (``to_dict`` order, angles in degrees), then
+    the grain temperature law of every component (``T_0.<label>``, then ``delta.<label>``), then
+    the interpolated calibration.  Step ``rel_step * max(|p|, 1)``.  Returns (names, gradient,
+    loss).
+    """
+    import dataclasses
+
+    base = ref.model_registry.model_registry.get_model(model_name)
+    cal0 = reference_rrm_calibration(ref, model_name, x_model, weights)
+
+    def loss(model, cal):
+        out = reference_evaluate(ref, model, u, obs, earth, bb_table, x_model, weights, degree,
+                                 scalars={"calibration": cal})
+        return float(np.dot(a, out.sum(axis=0)))
+
+    names, grads = [], []
+    L0 = loss(base, cal0)
+    for label, comp in base.comps.items():
+        init = {f.name: getattr(comp, f.name) for f in dataclasses.fields(comp) if f.init}
+        for key, val in init.items():
+            h = rel_step * max(abs(float(val)), 1.0)
+            vals = []
+            for sgn in (1, -1):
+                comps = dict(base.comps)
+                comps[label] = type(comp)(**{**init, key: float(val) + sgn * h})
+                vals.append(loss(dataclasses.replace(base, comps=comps), cal0))
+            names.append(f"comps.{label.value}.{key}")
+            grads.append((vals[0] - vals[1]) / (2 * h))
+    for field in ("T_0", "delta"):
+        table = getattr(base, field)
+        for label in base.comps:
+            v0 = float(table[label])
+            h = rel_step * max(abs(v0), 1.0)
+            vals = [loss(dataclasses.replace(base, **{field: {**table, label: v0 + sgn * h}}), cal0) for sgn in (1, -1)]
+            names.append(f"{field}.{label.value}")
+            grads.append((vals[0] - vals[1]) / (2 * h))
+    h = rel_step * max(abs(cal0), 1.0)
+    vals = [loss(base, cal0 + sgn * h) for sgn in (1, -1)]
+    names.append("calibration")
+    grads.append((vals[0] - vals[1]) / (2 * h))
+    return names, np.asarray(grads), L0

@@ -3,7 +3,7 @@
 Run with the path of a ZodiPy v1.1.3 source tree (the directory that holds
 ``zodipy/``), given as ``--ref PATH`` or in $ZODIPY_REF_ROOT:
 
-    python tests/golden/make_golden.py --ref PATH [grid | rrm | configs]
+    python tests/golden/make_golden.py --ref PATH [grid | rrm | rrm-grad | configs]
 
 The reference's own numeric modules are executed in place under an astropy
 stand-in (oracle/ref_loader.py).  Inputs that the reference would get from
@@ -19,7 +19,8 @@ those inputs to the per-component emission.  Outputs:
   grid_<case>.npz     inputs + reference grid_number_density output
 
 ``... grid`` regenerates only the grid fixtures, ``... rrm`` only
-ref_models.json and the RRM fixtures, ``... configs`` only the fixtures on the
+ref_models.json and the RRM fixtures, ``... rrm-grad`` only the RRM gradient
+fixtures, ``... configs`` only the fixtures on the
 benchmark configurations' inputs (los_cfg*.npz).
 """
 
@@ -42,6 +43,7 @@ from oracle.ref_loader import (  # noqa: E402
     load_reference,
     reference_evaluate,
     reference_fd_gradient,
+    reference_fd_gradient_rrm,
     reference_rrm_calibration,
     reference_spectral_scalars,
 )
@@ -266,6 +268,38 @@ def make_config_cases(ref) -> None:
         np.savez_compressed(os.path.join(HERE, f"los_{key}.npz"), **payload)
 
 
+def make_rrm_gradients(ref) -> None:
+    """Central finite differences of L = sum_i a_i total_i through the reference's own RRM code
+    (grad_rrm*.npz): every component parameter, T_0 and delta of every component, the
+    calibration."""
+    earth_2022 = earth_position(iso_to_mjd("2022-01-01T00:00:00"))
+    cases = {
+        # observer at 1 AU: inside the fan, below the bands and the comet
+        "rrm25": (25.0, random_sphere(24, seed=31), [0.9833, 0.0, 0.0]),
+        # just outside the fan's outer cutoff: the observer sits among the bands
+        "rrm60_belt": (60.0, random_sphere(24, seed=32), [1.9, -1.1, 0.04]),
+    }
+    for key, (x, u, obs) in cases.items():
+        obs = np.asarray(obs, dtype=np.float64)
+        bb = zodi_oracle.planck_table(x, None, unit="micron")
+        a = np.random.default_rng(98).uniform(0.5, 1.5, u.shape[1])
+        names, grad, L0 = reference_fd_gradient_rrm(ref, "rrm-experimental", u, obs, earth_2022, bb,
+                                                    np.asarray(x, dtype=np.float64), None, 50, a)
+        np.savez_compressed(
+            os.path.join(HERE, f"grad_{key}.npz"),
+            model=np.array("rrm-experimental"),
+            x=np.atleast_1d(np.float64(x)),
+            user_unit=np.array("micron"),
+            unit_vectors=u,
+            obs=obs,
+            earth=np.asarray(earth_2022, dtype=np.float64),
+            weights_a=a,
+            names=np.array(names),
+            fd_grad=grad,
+            loss=np.array(L0),
+        )
+
+
 def parse_args(argv):
     """(reference root, remaining words): ``--ref PATH`` wins over $ZODIPY_REF_ROOT."""
     argv = list(argv)
@@ -295,10 +329,16 @@ def main() -> None:
         with open(os.path.join(HERE, "ref_models.json"), "w") as f:
             json.dump(dump_models(ref), f, indent=1)
         make_rrm(ref)
+        make_rrm_gradients(ref)
         print("wrote RRM fixtures to", HERE)
+        return
+    if sys.argv[1:] == ["rrm-grad"]:
+        make_rrm_gradients(ref)
+        print("wrote RRM gradient fixtures to", HERE)
         return
     make_grids(ref)
     make_rrm(ref)
+    make_rrm_gradients(ref)
     make_config_cases(ref)
     models = dump_models(ref)
     with open(os.path.join(HERE, "ref_models.json"), "w") as f:

@@ -122,9 +122,8 @@ def test_adjoint_deterministic_across_launch_shapes(lib):
     g = torch.randn((2, adj.u.shape[1]), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(1))
     outs = []
     for bps in (0, 1, 3, 8):
-        _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, bps), "set_launch")
-        outs.append(engine.backward(zl, adj.u, adj.obs_dev, 1, g_total=g).cpu().numpy())
-    _lib.check(lib.zl_set_launch(_lib.ZL_PREC_F32, 0, 0), "set_launch")
+        opt = engine.launch_options(blocks_per_sm=bps)
+        outs.append(engine.backward(zl, adj.u, adj.obs_dev, 1, g_total=g, launch=opt).cpu().numpy())
     for o in outs[1:]:
         np.testing.assert_array_equal(o, outs[0])
 
@@ -217,11 +216,8 @@ def test_paired_adjoint_equals_scalar_kernel(lib, bands, per_comp):
     shape = (len(bands), zl.n_comps, n) if per_comp else (len(bands), n)
     g = 0.5 + torch.rand(shape, dtype=torch.float64, device="cuda", generator=gen)
     kw = {"g_comps": g} if per_comp else {"g_total": g}
-    try:
-        _lib.check(lib.zl_debug_one_pixel(1), "scalar kernels")
-        ref = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
-    finally:
-        _lib.check(lib.zl_debug_one_pixel(0), "default kernels")
+    ref = engine.backward(zl, dirs, obs, 1, launch=engine.launch_options(kernel=_lib.ZL_KERNEL_ONE_PIXEL), **kw)
+    ref = ref.cpu().numpy()
     got = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
     names = params.names(zl, models[0].comp_labels)
     theta = params.vector_from_model(zl)
@@ -261,11 +257,8 @@ def test_paired_adjoint_band_tails_healpix_order(lib, bands, per_comp):
     shape = (len(bands), zl.n_comps, n) if per_comp else (len(bands), n)
     g = 0.5 + torch.rand(shape, dtype=torch.float64, device="cuda", generator=gen)
     kw = {"g_comps": g} if per_comp else {"g_total": g}
-    try:
-        _lib.check(lib.zl_debug_one_pixel(1), "scalar kernels")
-        ref = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
-    finally:
-        _lib.check(lib.zl_debug_one_pixel(0), "default kernels")
+    ref = engine.backward(zl, dirs, obs, 1, launch=engine.launch_options(kernel=_lib.ZL_KERNEL_ONE_PIXEL), **kw)
+    ref = ref.cpu().numpy()
     got = engine.backward(zl, dirs, obs, 1, **kw).cpu().numpy()
     names = params.names(zl, models[0].comp_labels)
     scale = np.maximum(np.abs(params.vector_from_model(zl)), 1.0)

@@ -64,30 +64,64 @@ def test_batch_matches_oracle(lib):
 
 
 def test_graph_replay_equals_eager_and_launch_shape_does_not_matter(lib):
+    """Static and work-queue launches, tile sizes, sorted or input order, eager or replayed
+    from a CUDA graph (several replays on the same self-resetting queue): the same bits."""
     import torch
 
     from zodipy_gb300.batch import BatchEvaluator
 
     model, obs, counts, uu, earth = _setup(n_obs=9, lo=2000, hi=9000)
+    plain = BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32", sort=False)
+    plain.set_launch(64, 0, 0)
+    ref = plain.run().clone()
     ev = BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
-    ev.set_launch(64, 3)
-    eager = ev.run().clone()
-    ev.set_launch(128, 8)
+    for launch in ((64, 3, 64), (128, 0, 0), (128, 8, 512)):
+        ev.set_launch(*launch)
+        np.testing.assert_array_equal(ev.run().cpu().numpy(), ref.cpu().numpy())
     ev.capture()
-    ev.total.zero_()
-    ev.replay()
-    torch.cuda.synchronize()
-    np.testing.assert_array_equal(ev.total.cpu().numpy(), eager.cpu().numpy())
+    for _ in range(3):
+        ev.total.zero_()
+        ev.replay()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(ev.total.cpu().numpy(), ref.cpu().numpy())
+    assert ev.queue.cpu().tolist() == [0, 0]
 
 
-def test_autotuner_picks_a_valid_shape(lib, tmp_path, monkeypatch):
+def test_sorted_batch_skips_band_tails(lib):
+    """Sorting each observer's directions by latitude makes warps coherent: the share of
+    (warp, node) pairs at which the bands are zero for the whole warp goes from ~0 to a
+    large fraction (the kernel then skips them, with the same results)."""
+    from conftest import band_tail_share
+    from zodipy_gb300.batch import BatchEvaluator
+
+    model, obs, counts, uu, earth = _setup(n_obs=2, lo=40000, hi=40000)
+    ev = BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
+    u0 = uu[:, : counts[0]].cpu().numpy()
+    s0 = ev.u[:, : counts[0]].cpu().numpy()
+    assert band_tail_share(u0, obs[:, 0], warp=64) < 0.02
+    assert band_tail_share(s0, obs[:, 0], warp=64) > 0.2
+    np.testing.assert_array_equal(np.sort(s0[2]), s0[2])
+
+
+def test_tuning_one_evaluator_leaves_other_calls_alone(lib, tmp_path, monkeypatch):
+    """The autotuner picks a candidate shape and keeps it in its own evaluator: a Model
+    evaluated meanwhile, and another evaluator, keep their launches and results."""
     from zodipy_gb300 import batch
 
     monkeypatch.setattr(batch, "CACHE_PATH", str(tmp_path / "tune.json"))
     model, obs, counts, uu, earth = _setup(n_obs=4, lo=20000, hi=40000)
+    other = batch.BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
+    other.set_launch(96, 0, 0)
+    before = other.run().cpu().numpy().copy()
+    probe = uu[:, :500]
+    m_before = model.evaluate_xyz(probe, obs[:, 0], earth, return_comps=True, precision="float32").cpu().numpy()
     ev = batch.BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
-    tpb, bps, ms = ev.autotune(sample=1 << 16, reps=1)
-    assert tpb in batch.TPB_CHOICES and bps in batch.BPS_CHOICES and ms > 0
+    tpb, bps, tile, ms = ev.autotune(sample=1 << 16, reps=1)
+    assert (tpb, bps, tile) in batch.STATIC_CHOICES + batch.QUEUE_CHOICES and ms > 0
+    assert ev.launch == (tpb, bps, tile) and other.launch == (96, 0, 0)
     again = ev.autotune(sample=1 << 16, reps=1)  # from the cache
-    assert tuple(again[:2]) == (tpb, bps)
-    ev.set_launch(0, 0)
+    assert tuple(again[:3]) == (tpb, bps, tile)
+    np.testing.assert_array_equal(other.run().cpu().numpy(), before)
+    m_after = model.evaluate_xyz(probe, obs[:, 0], earth, return_comps=True, precision="float32").cpu().numpy()
+    np.testing.assert_array_equal(m_after, m_before)
+    np.testing.assert_array_equal(ev.run().cpu().numpy(), before)

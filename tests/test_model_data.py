@@ -178,7 +178,7 @@ def test_rrm_calibration_unpacking():
         np.testing.assert_allclose(m._b_nu_table, z["bb_table"], rtol=1e-13)
 
 
-def test_rrm_parameters_round_trip_and_adjoint_refusal(lib):
+def test_rrm_parameters_round_trip_and_gradient_layout(lib):
     import zodipy_gb300 as zg
     from zodipy_gb300 import _lib, engine
     from zodipy_gb300 import units as u
@@ -193,8 +193,15 @@ def test_rrm_parameters_round_trip_and_adjoint_refusal(lib):
     assert m.zl_model.comp_T_0[0] == 260.0 and m.zl_model.comp[0].p[2] == 11.0
     # the fan no longer shares its temperature law with anything, and the bands still share one range
     assert m.zl_model.comp[2].range == m.zl_model.comp[3].range == m.zl_model.comp[4].range
-    with pytest.raises(_lib.ZodiGBError, match="Kelsall"):
-        engine.grad_count(m.zl_model)
+    # the adjoint's gradient vector: every component's parameters, every T_0 and delta, the calibration
+    from zodipy_gb300 import params
+
+    n = engine.grad_count(m.zl_model)
+    assert n == params.size(m.zl_model) == len(params.names(m.zl_model, m.comp_labels)) == 99
+    v = params.vector_from_model(m.zl_model)
+    np.testing.assert_array_equal(params.vector_from_model(params.model_from_vector(m.zl_model, v)), v)
+    assert engine.backward_workspace_bytes(m.zl_model, 1000) == 8 * 8 * 20 * 8  # comps x tiles x slots x 8 B
+    assert isinstance(_lib.ZL_RRM, int)
 
 
 def test_model_set_rejects_incompatible_models(lib):

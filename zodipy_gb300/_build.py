@@ -31,6 +31,7 @@ SOURCES = [
     "zl_bwd_f32_dirbe.cu",
     "zl_bwd_dirbe_cp.cu",
     "zl_bwd_f32_planck.cu",
+    "zl_bwd_rrm.cu",
     "zl_diag.cu",
     "zl_static.cu",
     "zl_tod.cu",

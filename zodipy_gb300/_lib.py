@@ -12,7 +12,7 @@ import os
 
 from ._build import LIB_PATH
 
-ZL_ABI_VERSION = 2
+ZL_ABI_VERSION = 3
 ZL_MAX_COMPS = 8
 ZL_MAX_RANGES = 8
 ZL_MAX_SPEC = 4
@@ -25,6 +25,7 @@ ZL_KELSALL, ZL_RRM = 0, 1
 ZL_SEMB_L2_SCRATCH = 1024
 ZL_PREC_F64, ZL_PREC_F32 = 0, 1
 ZL_OK, ZL_ERR_ARG, ZL_ERR_CUDA, ZL_ERR_MODEL, ZL_ERR_SPACE = 0, -1, -2, -3, -4
+ZL_KERNEL_AUTO, ZL_KERNEL_ONE_PIXEL, ZL_KERNEL_TWO_PIXEL, ZL_KERNEL_PLAIN_GEOMETRY = 0, 1, 2, 3
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
 
@@ -89,6 +90,21 @@ class ZlObserver(ctypes.Structure):
     ]
 
 
+class ZlLaunch(ctypes.Structure):
+    """Launch options of one call (include/zodigb.h); all zero = the defaults."""
+
+    _fields_ = [
+        ("threads_per_block", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+        ("kernel", ctypes.c_int32),
+        ("band_tails", ctypes.c_int32),
+        ("tile", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("queue_dev", ctypes.c_void_p),
+        ("out_index_dev", ctypes.c_void_p),
+    ]
+
+
 # Every symbol the header declares, with its ctypes signature.
 _SIGNATURES = {
     "zl_abi_version": (ctypes.c_int, []),
@@ -109,7 +125,21 @@ _SIGNATURES = {
             ctypes.c_void_p,
         ],
     ),
-    "zl_set_launch": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "zl_forward_ex": (
+        ctypes.c_int,
+        [
+            ctypes.POINTER(ZlModel),
+            ctypes.c_void_p,
+            ctypes.c_int64,
+            ctypes.c_void_p,
+            ctypes.c_int32,
+            ctypes.c_int32,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+            ctypes.POINTER(ZlLaunch),
+            ctypes.c_void_p,
+        ],
+    ),
     "zl_forward_tod": (
         ctypes.c_int,
         [ctypes.POINTER(ZlModel), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -164,6 +194,23 @@ _SIGNATURES = {
             ctypes.c_void_p,
         ],
     ),
+    "zl_backward_ex": (
+        ctypes.c_int,
+        [
+            ctypes.POINTER(ZlModel),
+            ctypes.c_void_p,
+            ctypes.c_int64,
+            ctypes.c_void_p,
+            ctypes.c_int32,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+            ctypes.c_void_p,
+            ctypes.c_size_t,
+            ctypes.POINTER(ZlLaunch),
+            ctypes.c_void_p,
+        ],
+    ),
     "zl_grad_count": (ctypes.c_int, [ctypes.POINTER(ZlModel), ctypes.POINTER(ctypes.c_int32)]),
     "zl_backward_workspace_bytes": (ctypes.c_int, [ctypes.POINTER(ZlModel), ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "zl_backward": (
@@ -182,8 +229,6 @@ _SIGNATURES = {
             ctypes.c_void_p,
         ],
     ),
-    "zl_debug_plain_geometry": (ctypes.c_int, [ctypes.c_int32]),
-    "zl_debug_one_pixel": (ctypes.c_int, [ctypes.c_int32]),
     "zl_mapped_pointer": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "zl_diag_pipe_probe": (
         ctypes.c_int,

@@ -7,24 +7,25 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "zl_common.cuh"
 
 namespace zl {
 cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
-                           double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
-extern int g_two_pixel_dirbe;
-extern int g_bwd_unpaired;
-cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, bool one_pixel, const double* u, int64_t n,
-                           const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb,
-                           int bps, int num_sms);
+                           double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
+cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, int kernel, bool tails, const double* u, int64_t n,
+                           const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 int grad_count_layout(int layout, int n_spec);
 int bwd_groups(int layout);
-cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
-                           const ObsArgs& obs, const double* g_comps, const double* g_total,
+cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, bool unpaired, const double* u,
+                           int64_t n, const ObsArgs& obs, const double* g_comps, const double* g_total,
                            double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms);
 cudaError_t launch_reduce_tiles(const double* partials, int64_t n_rows, int ng, double* out, cudaStream_t st);
+int rrm_grad_count(const ZlModel& m);
+cudaError_t launch_bwd_rrm(const ZlModel& m, const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
+                           const double* g_comps, const double* g_total, double* partials, int64_t n_tiles,
+                           double* grad_out, cudaStream_t st, int bps, int num_sms);
+constexpr int kRrmPartialSlots = 20;  // doubles per component and tile (zl_bwd_rrm.cu)
 cudaError_t launch_tod_flags(const ZlModel& m, const double* obs, int64_t n, uint32_t* flags, cudaStream_t st,
                              int num_sms);
 cudaError_t launch_density_grid(const ZlModel& M, const double* x, int nx, const double* y, int ny, const double* z,
@@ -62,15 +63,10 @@ int cuda_fail(cudaError_t e, const char* what) {
   return fail(ZL_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
-struct LaunchCfg {
-  int tpb = 128;
-  int bps = 0;  // 0 = the library default of the entry point
-};
 // blocks per SM large enough that every launcher's grid reaches its cap of one block per
 // 128 pixels (or tiles) for any map below ~1.3e9 pixels; bounds the grid at 152 x 65536 blocks
 constexpr int kBpsOnePixelPerThread = 1 << 16;
-LaunchCfg g_cfg[2];
-std::mutex g_mu;
+constexpr int kMaxQueueTile = 1 << 20;
 
 // SM count of the current device, queried once per device and cached so that
 // launches recorded into a CUDA graph make no device queries.
@@ -160,18 +156,28 @@ extern "C" ZL_API int zl_observer_flags(const ZlModel* m, ZlObserver* obs, int64
   return ZL_OK;
 }
 
-extern "C" ZL_API int zl_set_launch(int32_t precision, int32_t tpb, int32_t bps) {
-  if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
-  if (tpb != 0 && (tpb < 32 || tpb > 128 || tpb % 32)) return fail(ZL_ERR_ARG, "threads_per_block %d not in {32..128 step 32}", tpb);
-  if (bps < 0 || bps > kBpsOnePixelPerThread)
-    return fail(ZL_ERR_ARG, "blocks_per_sm %d out of [0,%d]", bps, kBpsOnePixelPerThread);
-  std::lock_guard<std::mutex> g(g_mu);
-  g_cfg[precision].tpb = tpb ? tpb : 128;
-  g_cfg[precision].bps = bps;
+namespace {
+
+// A call's launch options, checked, with the defaults filled in (NULL = all defaults).
+int launch_options(const ZlLaunch* in, ZlLaunch* out) {
+  ZlLaunch d;
+  memset(&d, 0, sizeof(d));
+  if (in) d = *in;
+  if (d.threads_per_block == 0) d.threads_per_block = 128;
+  if (d.threads_per_block < 32 || d.threads_per_block > 128 || d.threads_per_block % 32)
+    return fail(ZL_ERR_ARG, "threads_per_block %d not in {32..128 step 32}", d.threads_per_block);
+  if (d.blocks_per_sm < 0 || d.blocks_per_sm > kBpsOnePixelPerThread)
+    return fail(ZL_ERR_ARG, "blocks_per_sm %d out of [0,%d]", d.blocks_per_sm, kBpsOnePixelPerThread);
+  if (d.kernel < ZL_KERNEL_AUTO || d.kernel > ZL_KERNEL_PLAIN_GEOMETRY) return fail(ZL_ERR_ARG, "bad kernel %d", d.kernel);
+  if (d.band_tails != 0 && d.band_tails != 1) return fail(ZL_ERR_ARG, "band_tails %d not 0 or 1", d.band_tails);
+  if (d.tile < 0 || d.tile > kMaxQueueTile) return fail(ZL_ERR_ARG, "tile %d out of [0,%d]", d.tile, kMaxQueueTile);
+  if (d.tile > 0 && (d.tile % d.threads_per_block))
+    return fail(ZL_ERR_ARG, "tile %d is not a multiple of threads_per_block %d", d.tile, d.threads_per_block);
+  if (d.tile > 0 && !d.queue_dev) return fail(ZL_ERR_ARG, "tile > 0 needs queue_dev");
+  if (d.tile == 0) d.queue_dev = nullptr;
+  *out = d;
   return ZL_OK;
 }
-
-namespace {
 
 void first_in_range(const ZlModel& m, int32_t* out) {
   for (int c = 0; c < m.n_comps; ++c) out[c] = (c == 0 || m.comp[c].range != m.comp[c - 1].range) ? 1 : 0;
@@ -393,57 +399,40 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
 
 }  // namespace
 
-// Testing hook: 1 selects the all-float32 geometry variant of the DIRBE-layout
-// kernel (no float-float near the ring and feature).  Not part of the ABI.
-static int g_plain_geometry = 0;
-extern "C" ZL_API int zl_debug_plain_geometry(int32_t on) {
-  g_plain_geometry = on ? 1 : 0;
-  return ZL_OK;
-}
-
-// Testing hook: 1 keeps the one-pixel, unpaired float32 kernels (forward and
-// adjoint) where the packed f32x2 kernels would run, so the two can be compared.
-// Not part of the ABI.
-static int g_one_pixel = 0;
-extern "C" ZL_API int zl_debug_one_pixel(int32_t on) {
-  g_one_pixel = on > 0 ? 1 : 0;
-  zl::g_bwd_unpaired = g_one_pixel;
-  zl::g_two_pixel_dirbe = on < 0 ? 1 : 0;  // -1: two-pixel kernel for the DIRBE layout too
-  return ZL_OK;
-}
-
 namespace {
 
-// zl_forward / zl_forward_tod after the observer source is set up.
+// zl_forward / zl_forward_ex / zl_forward_tod after the observer source is set up.
 int forward_impl(const ZlModel* model, const double* u, int64_t n_pix, const ObsArgs& OA, int32_t precision,
-                 double* out_comps, double* out_total, void* stream) {
+                 double* out_comps, double* out_total, const ZlLaunch* launch, void* stream) {
   int rc = 0;
   if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
   if (!out_comps && !out_total) return fail(ZL_ERR_ARG, "both outputs are NULL");
   if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
+  ZlLaunch opt;
+  if ((rc = launch_options(launch, &opt))) return rc;
+  // the queue's counter is 32-bit: every tile plus each block's final fetch must fit
+  if (opt.queue_dev && n_pix / opt.tile >= (int64_t)1 << 30)
+    return fail(ZL_ERR_ARG, "%lld pixels in tiles of %d overflow the work queue", (long long)n_pix, opt.tile);
   int nsm = 0;
   if ((rc = sm_count(&nsm))) return rc;
-  LaunchCfg cfg;
-  {
-    std::lock_guard<std::mutex> g(g_mu);
-    cfg = g_cfg[precision];
-  }
+  LaunchArgs L{opt.threads_per_block, opt.blocks_per_sm, nsm, Sched{opt.queue_dev, opt.tile, opt.out_index_dev}};
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
   if (precision == ZL_PREC_F64) {
     static thread_local KParamsF64 P;
     build_f64(*model, &P);
-    const int bps = cfg.bps ? cfg.bps : 8;
-    e = launch_fwd_f64(P, u, n_pix, OA, out_comps, out_total, st, cfg.tpb, bps, nsm);
+    if (!L.bps) L.bps = 8;
+    e = launch_fwd_f64(P, u, n_pix, OA, out_comps, out_total, st, L);
   } else {
     static thread_local KParamsF32 P;
     build_f32(*model, &P);
-    // default: one pixel per thread.  Pixels cost different amounts (a warp whose pixels are all
-    // past a band's zero tail skips it), so many short blocks balance the SMs better than a few
-    // long-running ones (DIRBE 25 um at nside 512: 1.48 ms with 8 blocks per SM, 1.33 ms).
-    const int bps = cfg.bps ? cfg.bps : kBpsOnePixelPerThread;
-    e = launch_fwd_f32(P, detect_layout(*model), g_plain_geometry != 0, g_one_pixel != 0, u, n_pix, OA, out_comps,
-                       out_total, st, cfg.tpb, bps, nsm);
+    // default: one block per tile (one pixel or pixel pair per thread) without a queue.  Pixels
+    // cost different amounts (a warp whose pixels are all past a band's zero tail skips it), so
+    // many short blocks balance the SMs better than a few long-running ones (DIRBE 25 um at nside
+    // 512: 1.48 ms with 8 blocks per SM, 1.33 ms); a queued launch defaults to 8 blocks per SM.
+    if (!L.bps) L.bps = opt.queue_dev ? 8 : kBpsOnePixelPerThread;
+    e = launch_fwd_f32(P, detect_layout(*model), opt.kernel, opt.band_tails != 0, u, n_pix, OA, out_comps, out_total,
+                       st, L);
   }
   if (e != cudaSuccess) return cuda_fail(e, "zl_forward launch");
   return ZL_OK;
@@ -479,7 +468,20 @@ extern "C" ZL_API int zl_forward(const ZlModel* model, const double* u, int64_t 
   if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
   if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
   const ObsArgs OA{obs, n_obs, nullptr, nullptr, nullptr};
-  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, stream);
+  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, nullptr, stream);
+}
+
+extern "C" ZL_API int zl_forward_ex(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs,
+                                    int32_t n_obs, int32_t precision, double* out_comps, double* out_total,
+                                    const ZlLaunch* launch, void* stream) {
+  int rc = zl_model_check(model);
+  if (rc) return rc;
+  if (n_pix < 0) return fail(ZL_ERR_ARG, "n_pix < 0");
+  if (n_pix == 0) return ZL_OK;
+  if (!u) return fail(ZL_ERR_ARG, "unit_vectors is NULL");
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  const ObsArgs OA{obs, n_obs, nullptr, nullptr, nullptr};
+  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, launch, stream);
 }
 
 extern "C" ZL_API int zl_forward_tod(const ZlModel* model, const double* u, int64_t n_pix, const double* obs_xyz,
@@ -494,7 +496,7 @@ extern "C" ZL_API int zl_forward_tod(const ZlModel* model, const double* u, int6
   if (precision != ZL_PREC_F64 && precision != ZL_PREC_F32) return fail(ZL_ERR_ARG, "bad precision %d", precision);
   ObsArgs OA;
   if ((rc = tod_setup(model, n_pix, obs_xyz, earth_xyz, flags, stream, &OA))) return rc;
-  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, stream);
+  return forward_impl(model, u, n_pix, OA, precision, out_comps, out_total, nullptr, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -506,8 +508,13 @@ constexpr int kBwdTile = 128;
 
 int64_t bwd_tiles(int64_t n_pix) { return (n_pix + kBwdTile - 1) / kBwdTile; }
 
+// Adjoint kernel family of a model: the Kelsall layouts 1 (DIRBE) and 2 (Planck), or -1 for an
+// RRM model (one launch per component, zl_bwd_rrm.cu).
 int bwd_layout(const ZlModel& m, int* layout) {
-  if (m.family != ZL_KELSALL) return fail(ZL_ERR_MODEL, "the adjoint supports Kelsall models only (this is an RRM model)");
+  if (m.family == ZL_RRM) {
+    *layout = -1;
+    return ZL_OK;
+  }
   const int l = detect_layout(m);
   if (l == 0)
     return fail(ZL_ERR_MODEL,
@@ -580,7 +587,7 @@ extern "C" ZL_API int zl_grad_count(const ZlModel* model, int32_t* count) {
   if (!count) return fail(ZL_ERR_ARG, "count is NULL");
   int layout = 0;
   if ((rc = bwd_layout(*model, &layout))) return rc;
-  *count = grad_count_layout(layout, model->n_spec);
+  *count = layout < 0 ? rrm_grad_count(*model) : grad_count_layout(layout, model->n_spec);
   return ZL_OK;
 }
 
@@ -590,6 +597,10 @@ extern "C" ZL_API int zl_backward_workspace_bytes(const ZlModel* model, int64_t 
   if (!bytes || n_pix < 0) return fail(ZL_ERR_ARG, "bytes is NULL or n_pix < 0");
   int layout = 0;
   if ((rc = bwd_layout(*model, &layout))) return rc;
+  if (layout < 0) {
+    *bytes = (size_t)model->n_comps * (size_t)bwd_tiles(n_pix) * kRrmPartialSlots * sizeof(double);
+    return ZL_OK;
+  }
   const int ng = grad_count_layout(layout, model->n_spec);
   *bytes = (size_t)bwd_groups(layout) * (size_t)bwd_tiles(n_pix) * ng * sizeof(double);
   return ZL_OK;
@@ -599,32 +610,42 @@ namespace {
 
 int backward_impl(const ZlModel* model, int layout, const double* u, int64_t n_pix, const ObsArgs& OA,
                   const double* g_comps, const double* g_total, double* grad_out, void* workspace,
-                  size_t workspace_bytes, void* stream) {
+                  size_t workspace_bytes, const ZlLaunch* launch, void* stream) {
   int rc = 0;
+  ZlLaunch opt;
+  if ((rc = launch_options(launch, &opt))) return rc;
+  if (opt.kernel != ZL_KERNEL_AUTO && opt.kernel != ZL_KERNEL_ONE_PIXEL)
+    return fail(ZL_ERR_ARG, "the adjoint has no kernel %d", opt.kernel);
   size_t need = 0;
   if ((rc = zl_backward_workspace_bytes(model, n_pix, &need))) return rc;
   if (workspace_bytes < need || (need > 0 && !workspace))
     return fail(ZL_ERR_SPACE, "workspace of %zu bytes is smaller than the %zu required", workspace_bytes, need);
   int nsm = 0;
   if ((rc = sm_count(&nsm))) return rc;
-  int bps = 0;
-  {
-    std::lock_guard<std::mutex> g(g_mu);
-    bps = g_cfg[ZL_PREC_F32].bps;
-  }
   // default: 96 blocks per SM, 1.7 tiles per block at nside 512 (per-tile cost varies as in the
   // forward; 2.62 ms with 4 blocks per SM, 2.39 ms)
-  if (bps <= 0) bps = 96;
+  const int bps = opt.blocks_per_sm > 0 ? opt.blocks_per_sm : 96;
   cudaStream_t st = (cudaStream_t)stream;
-  const int ng = grad_count_layout(layout, model->n_spec);
   const int64_t n_tiles = bwd_tiles(n_pix);
   double* partials = (double*)workspace;
   static thread_local KParamsF32 P;
-  static thread_local KGradAux A;
   build_f32(*model, &P);
+  if (layout < 0) {  // RRM: one launch per component, then the fixed-order reduction
+    if (n_tiles == 0) {
+      const cudaError_t z = cudaMemsetAsync(grad_out, 0, sizeof(double) * rrm_grad_count(*model), st);
+      return z == cudaSuccess ? ZL_OK : cuda_fail(z, "zl_backward zero gradient");
+    }
+    const cudaError_t er = launch_bwd_rrm(*model, P, u, n_pix, OA, g_comps, g_total, partials, n_tiles, grad_out, st,
+                                          bps, nsm);
+    return er == cudaSuccess ? ZL_OK : cuda_fail(er, "zl_backward launch (RRM)");
+  }
+  const int ng = grad_count_layout(layout, model->n_spec);
+  static thread_local KGradAux A;
   build_aux(*model, &A);
   cudaError_t e = cudaSuccess;
-  if (n_tiles > 0) e = launch_bwd_f32(P, A, layout, u, n_pix, OA, g_comps, g_total, partials, n_tiles, st, bps, nsm);
+  if (n_tiles > 0)
+    e = launch_bwd_f32(P, A, layout, opt.kernel == ZL_KERNEL_ONE_PIXEL, u, n_pix, OA, g_comps, g_total, partials,
+                       n_tiles, st, bps, nsm);
   if (e != cudaSuccess) return cuda_fail(e, "zl_backward launch");
   e = launch_reduce_tiles(partials, n_tiles * bwd_groups(layout), ng, grad_out, st);
   if (e != cudaSuccess) return cuda_fail(e, "zl_backward reduce");
@@ -653,7 +674,20 @@ extern "C" ZL_API int zl_backward(const ZlModel* model, const double* u, int64_t
   if (rc) return rc;
   if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
   const ObsArgs OA{obs, n_obs, nullptr, nullptr, nullptr};
-  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, stream);
+  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, nullptr,
+                       stream);
+}
+
+extern "C" ZL_API int zl_backward_ex(const ZlModel* model, const double* u, int64_t n_pix, const ZlObserver* obs,
+                                     int32_t n_obs, const double* g_comps, const double* g_total, double* grad_out,
+                                     void* workspace, size_t workspace_bytes, const ZlLaunch* launch, void* stream) {
+  int layout = 0;
+  int rc = backward_args(model, u, n_pix, g_comps, g_total, grad_out, &layout);
+  if (rc) return rc;
+  if (!obs || n_obs < 1) return fail(ZL_ERR_ARG, "observers: NULL or n_obs < 1");
+  const ObsArgs OA{obs, n_obs, nullptr, nullptr, nullptr};
+  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, launch,
+                       stream);
 }
 
 extern "C" ZL_API int zl_backward_tod(const ZlModel* model, const double* u, int64_t n_pix, const double* obs_xyz,
@@ -665,7 +699,8 @@ extern "C" ZL_API int zl_backward_tod(const ZlModel* model, const double* u, int
   if (rc) return rc;
   ObsArgs OA{nullptr, 0, nullptr, nullptr, nullptr};
   if (n_pix > 0 && (rc = tod_setup(model, n_pix, obs_xyz, earth_xyz, flags, stream, &OA))) return rc;
-  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, stream);
+  return backward_impl(model, layout, u, n_pix, OA, g_comps, g_total, grad_out, workspace, workspace_bytes, nullptr,
+                       stream);
 }
 
 // ---------------------------------------------------------------------------

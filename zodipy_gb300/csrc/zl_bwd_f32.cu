@@ -33,14 +33,17 @@ int grad_count_layout(int layout, int n_spec) {
 int bwd_groups(int layout) { return layout == 1 ? 2 : 1; }
 
 // partials: [bwd_groups(layout)][n_tiles][grad_count_layout(layout, n_spec)]
-cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, const double* u, int64_t n,
-                           const ObsArgs& obs, const double* g_comps, const double* g_total,
+// unpaired: the one-pixel kernel with components in order even where the component-paired
+// kernels would run (for comparing the two)
+cudaError_t launch_bwd_f32(const KParamsF32& P, const KGradAux& A, int layout, bool unpaired, const double* u,
+                           int64_t n, const ObsArgs& obs, const double* g_comps, const double* g_total,
                            double* partials, int64_t n_tiles, cudaStream_t st, int bps, int num_sms) {
   int64_t grid = (int64_t)num_sms * bps;
   if (grid > n_tiles) grid = n_tiles;
   if (grid < 1) grid = 1;
   const uint32_t flags = f32_flags(P, layout);
-  if (layout == 1) return launch_bwd_f32_dirbe(P, A, flags, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+  if (layout == 1)
+    return launch_bwd_f32_dirbe(P, A, flags, unpaired, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
   return launch_bwd_f32_planck(P, A, flags, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
 }
 

@@ -657,9 +657,9 @@ static cudaError_t launch_bwd_nspec(const KParamsF32& P, const KGradAux& A, cons
 // The backward reads every flag but scattering (that is its SCAT parameter).
 constexpr uint32_t kBwdFlagsMask = ~2u;
 
-cudaError_t launch_bwd_f32_dirbe(const KParamsF32& P, const KGradAux& A, uint32_t flags, const double* u, int64_t n,
-                                 const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
-                                 int64_t n_tiles, cudaStream_t st, int64_t grid);
+cudaError_t launch_bwd_f32_dirbe(const KParamsF32& P, const KGradAux& A, uint32_t flags, bool unpaired, const double* u,
+                                 int64_t n, const ObsArgs& obs, const double* g_comps, const double* g_total,
+                                 double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid);
 cudaError_t launch_bwd_f32_planck(const KParamsF32& P, const KGradAux& A, uint32_t flags, const double* u, int64_t n,
                                   const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
                                   int64_t n_tiles, cudaStream_t st, int64_t grid);

@@ -1,21 +1,20 @@
 // Adjoint kernels of the DIRBE component layout (cloud | 3 bands | ring | feature).
 // Models with the built-in flags take the component-paired kernels
 // (zl_bwd_dirbe_cp.cu); the scalar kernel reads the flags at run time and serves
-// every other DIRBE-layout model (and the comparison hook zl_debug_one_pixel).
+// every other DIRBE-layout model, and any model when the caller asks for the
+// one-pixel kernels (ZL_KERNEL_ONE_PIXEL, for comparing the two).
 #include "zl_bwd_f32.cuh"
 
 namespace zl {
-
-int g_bwd_unpaired = 0;
 
 cudaError_t launch_bwd_dirbe_cp(const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
                                 const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
                                 int64_t n_tiles, cudaStream_t st, int64_t grid);
 
-cudaError_t launch_bwd_f32_dirbe(const KParamsF32& P, const KGradAux& A, uint32_t flags, const double* u, int64_t n,
-                                 const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
-                                 int64_t n_tiles, cudaStream_t st, int64_t grid) {
-  if (!g_bwd_unpaired && (flags & kBwdFlagsMask) == (kFlagsKelsall & kBwdFlagsMask))
+cudaError_t launch_bwd_f32_dirbe(const KParamsF32& P, const KGradAux& A, uint32_t flags, bool unpaired, const double* u,
+                                 int64_t n, const ObsArgs& obs, const double* g_comps, const double* g_total,
+                                 double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
+  if (!unpaired && (flags & kBwdFlagsMask) == (kFlagsKelsall & kBwdFlagsMask))
     return launch_bwd_dirbe_cp(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
   return launch_bwd_nspec<kLayoutDirbe, kFlagsRuntime>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
 }

@@ -173,7 +173,7 @@ __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return {a.hi * pow2, 
 // splits nine doubles, so this works on the bits: the top 24 significand bits (truncated) and
 // the next 23 (made a float by setting them as the significand of 2^(E-23) and subtracting
 // 2^(E-23) exactly), renormalised so that hi is the rounded float value of d (as (float)d
-// gives it); 2^-47 relative.  The 6 significand bits below those 47 are not kept, but they
+// gives it); |hi + lo - d| < 2^-45 |d|.  The 6 significand bits below those 47 are not kept, but they
 // stick to the lowest kept bit (set it when any of them is set), so that a value just above a
 // halfway point between two floats still rounds up when the pair is renormalised, as
 // round-to-nearest of the double does; an exact halfway point rounds to even in both.
@@ -330,6 +330,116 @@ __device__ __forceinline__ PixObs pixel_observer(const ObsArgs& A, int64_t i, in
     p.outside = __ldg(A.flags);
   }
   return p;
+}
+
+// ---------------------------------------------------------------------------
+// How the blocks of a forward launch find their work (ZlLaunch of the C ABI).
+// A launch covers n_items items (pixels; pixel pairs for the two-pixel kernel) in
+// tiles of consecutive items:
+//  - static schedule (queue == NULL): tiles of blockDim.x items, block b taking tiles
+//    b, b + gridDim.x, ... -- the grid-stride loop;
+//  - work queue (queue != NULL): tiles of `tile` items pulled from a device counter,
+//    queue[0], by one atomic add per tile, until the items run out, so blocks that
+//    draw cheap tiles take more of them.  The blocks that find the queue empty count
+//    themselves out in queue[1]; the last one puts both words back to zero, so the
+//    next launch on the same queue (a CUDA-graph replay, say) starts from tile 0.
+//    No block ever waits for another, and results never depend on which block ran
+//    which tile.
+// out_index: output column of each pixel (NULL: the pixel's own index); lets a caller
+// run its pixels in another order (sorted for coherence) and still get its layout.
+// ---------------------------------------------------------------------------
+struct Sched {
+  unsigned int* queue;
+  int32_t tile;
+  const int64_t* out_index;
+};
+
+__device__ __forceinline__ int64_t out_col(const Sched& S, int64_t i) { return S.out_index ? S.out_index[i] : i; }
+
+// Items per tile of a launch.
+__device__ __forceinline__ int64_t sched_tile(const Sched& S) { return S.queue ? (int64_t)S.tile : (int64_t)blockDim.x; }
+
+// Schedules a kernel is compiled for: both (chosen by S.queue at run time), or one of them
+// (a kernel whose register count is tight compiles one instantiation per schedule).
+enum { kSchedAny = 0, kSchedStatic = 1, kSchedQueue = 2 };
+
+template <int MODE>
+__device__ __forceinline__ bool sched_queued(const Sched& S) {
+  return MODE == kSchedQueue || (MODE == kSchedAny && S.queue != nullptr);
+}
+
+// Next tile from the queue, the same for every thread of the block.
+__device__ __forceinline__ int64_t sched_fetch(const Sched& S) {
+  __shared__ unsigned int s_next;
+  __syncthreads();  // every thread has read s_next for the previous tile
+  if (threadIdx.x == 0) s_next = atomicAdd(S.queue, 1u);
+  __syncthreads();
+  return (int64_t)s_next;
+}
+
+// After a block's last tile: count the block out; the last one resets the queue.
+template <int MODE>
+__device__ __forceinline__ void sched_finish(const Sched& S) {
+  if (!sched_queued<MODE>(S) || threadIdx.x != 0) return;
+  __threadfence();
+  if (atomicAdd(S.queue + 1, 1u) == gridDim.x - 1) {
+    atomicExch(S.queue + 1, 0u);
+    atomicExch(S.queue, 0u);
+  }
+}
+
+// The loop of ZL_SCHED_LOOP.  Static: the grid-stride loop over items.  Queue: tb is the
+// first item of the block's current tile; every thread steps through the tile in blockDim
+// strides (tiles are a multiple of blockDim, so all threads reach the tile's end at the same
+// iteration) and the block fetches the next tile together.
+template <int MODE>
+__device__ __forceinline__ int64_t sched_base0(const Sched& S) {
+  return sched_queued<MODE>(S) ? sched_fetch(S) * (int64_t)S.tile : 0;
+}
+template <int MODE>
+__device__ __forceinline__ int64_t sched_i0(const Sched& S, int64_t tb) {
+  return (sched_queued<MODE>(S) ? tb : (int64_t)blockIdx.x * blockDim.x) + threadIdx.x;
+}
+template <int MODE>
+__device__ __forceinline__ bool sched_more(const Sched& S, int64_t i, int64_t tb, int64_t n_items) {
+  return sched_queued<MODE>(S) ? tb < n_items : i < n_items;
+}
+template <int MODE>
+__device__ __forceinline__ int64_t sched_next(const Sched& S, int64_t i, int64_t& tb) {
+  if (!sched_queued<MODE>(S)) return i + (int64_t)gridDim.x * blockDim.x;
+  i += blockDim.x;
+  if (i >= tb + S.tile) {
+    tb = sched_fetch(S) * (int64_t)S.tile;
+    i = tb + threadIdx.x;
+  }
+  return i;
+}
+
+// for (each item i of this block's tiles) { ... }: a plain loop rather than a function taking
+// the body as a lambda, whose closure cost the DIRBE forward kernel 17 registers.  With the queue,
+// every thread of the block runs the same iterations (items past n_items skip the body), since
+// the tile fetch synchronises the block.  Call sched_finish<MODE>(S) after the loop.
+#define ZL_SCHED_LOOP(MODE, S, n_items, i)                                                                 \
+  for (int64_t _zl_tb = ::zl::sched_base0<MODE>(S), i = ::zl::sched_i0<MODE>(S, _zl_tb);                \
+       ::zl::sched_more<MODE>(S, i, _zl_tb, (n_items)); i = ::zl::sched_next<MODE>(S, i, _zl_tb))        \
+    if (::zl::sched_queued<MODE>(S) && i >= (n_items)) continue;                                         \
+    else
+
+// Host side of a forward launch: block shape, grid sizing and the schedule.
+struct LaunchArgs {
+  int tpb;      // threads per block
+  int bps;      // blocks per SM the grid is capped at
+  int num_sms;
+  Sched sched;
+};
+
+// Grid of a launch over n_items: one block per tile, capped at num_sms x bps.
+inline int64_t fwd_grid(const LaunchArgs& L, int64_t n_items) {
+  const int64_t T = L.sched.queue ? (int64_t)L.sched.tile : (int64_t)L.tpb;
+  int64_t grid = (n_items + T - 1) / T;
+  const int64_t cap = (int64_t)L.num_sms * L.bps;
+  if (grid > cap) grid = cap;
+  return grid < 1 ? 1 : grid;
 }
 
 }  // namespace zl

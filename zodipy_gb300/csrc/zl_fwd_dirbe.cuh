@@ -65,17 +65,20 @@ __device__ __forceinline__ float band_y1(float R2, float inv_dr2) {
   return q8 * q2;
 }
 
-template <int NSPEC, uint32_t FLAGS>
-__global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant__ KParamsF32 P,
+// QUEUE: compiled for the work-queue schedule, else the static grid-stride loop (which keeps
+// the one-band kernel at 96 registers: five blocks per SM).
+template <int NSPEC, uint32_t FLAGS, bool QUEUE>
+__global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 1u)) ? 5 : 0) fwd_dirbe_cp_kernel(const __grid_constant__ KParamsF32 P,
                                                            const double* __restrict__ u, int64_t n_pix,
                                                            const ObsArgs OA, double* __restrict__ out_comps,
-                                                           double* __restrict__ out_total) {
+                                                           double* __restrict__ out_total, const Sched SC) {
   using Fl = KFlags<FLAGS>;
   static_assert(!Fl::runtime, "compiled flags only");
   static_assert(((FLAGS >> 8) & 0x3Fu) == 1u, "only the cloud is offset from the Sun");
   static_assert(((FLAGS >> 17) & 7u) == 7u, "bands with p = 4");
   static_assert(((FLAGS >> 25) & 7u) == 4u, "band 3 (only) reuses band 1's inner-cutoff term");
   constexpr int NC = 6;
+  constexpr int MODE = QUEUE ? kSchedQueue : kSchedStatic;
   extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
   const int nT = P.n_temps;
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
@@ -88,7 +91,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
   const KCompF32& Cr = P.comp[4];
   const KCompF32& Cf = P.comp[5];
 
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
+  ZL_SCHED_LOOP(MODE, SC, n_pix, i) {
     PixSetupF32<NC> PS;
     pixel_setup<kLayoutDirbe, FLAGS, true, NC>(P, u, n_pix, OA, i, PS);
     const ff2 z1b = pack_ff(PS.z1[1], PS.z1[2]), z0b = pack_ff(PS.z0[1], PS.z0[2]);
@@ -253,6 +256,7 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
     }
 
     // ---- outputs: x (stop - start)/2, component order total ------------------
+    const int64_t col = out_col(SC, i);
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s) {
       const float sums[NC] = {as0[s] - ac0[s], as12[s].x - ac12[s].x, as12[s].y - ac12[s].y,
@@ -264,28 +268,28 @@ __global__ void __launch_bounds__(128) fwd_dirbe_cp_kernel(const __grid_constant
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         const double v = (double)(sums[c] * hsc[c]);
-        if (out_comps) out_comps[((int64_t)s * NC + c) * n_pix + i] = v;
+        if (out_comps) out_comps[((int64_t)s * NC + c) * n_pix + col] = v;
         tot = (c == 0) ? v : __dadd_rn(tot, v);
       }
-      if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
+      if (out_total) out_total[(int64_t)s * n_pix + col] = tot;
     }
   }
+  sched_finish<MODE>(SC);
 }
 
 template <int NSPEC, uint32_t FLAGS>
 static cudaError_t launch_dirbe_cp_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
-                                     double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                                     double* ot, cudaStream_t st, const LaunchArgs& L) {
   const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
-  const int64_t blocks_needed = (n + tpb - 1) / tpb;
-  int64_t grid = (int64_t)num_sms * bps;
-  if (grid > blocks_needed) grid = blocks_needed;
-  if (grid < 1) grid = 1;
-  fwd_dirbe_cp_kernel<NSPEC, FLAGS><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
+  if (L.sched.queue)
+    fwd_dirbe_cp_kernel<NSPEC, FLAGS, true><<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
+  else
+    fwd_dirbe_cp_kernel<NSPEC, FLAGS, false><<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
   return cudaGetLastError();
 }
 
 // Launcher (zl_fwd_dirbe_cp.cu); cudaErrorNotSupported for a flag set it is not compiled for.
 cudaError_t launch_fwd_dirbe_cp(const KParamsF32& P, uint32_t flags, const double* u, int64_t n, const ObsArgs& obs,
-                                double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
+                                double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 
 }  // namespace zl

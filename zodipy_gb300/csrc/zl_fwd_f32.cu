@@ -24,32 +24,29 @@ uint32_t f32_flags(const KParamsF32& P, int layout) {
   return f;
 }
 
-int g_two_pixel_dirbe = 0;
-
-// layout: 1 = DIRBE-like, 2 = Planck-like, 0 = generic; plain_geometry selects the
-// all-float32 variant of the DIRBE layout (kept for the precision/speed study); one_pixel
-// keeps the one-pixel kernel where the two-pixel one (zl_fwd_f32x2.cuh) would run.
-cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, bool plain_geometry, bool one_pixel, const double* u,
-                           int64_t n, const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
-                           int num_sms) {
+// kernel (ZL_KERNEL_* of the C ABI): AUTO takes the fastest measured kernel of the layout --
+// the component-paired kernel for the DIRBE layout, the two-pixel kernel for the Planck layout
+// (measured on GB300 at nside 512: Planck layout 0.79 ms two-pixel vs 0.91 ms one-pixel; the
+// two-pixel DIRBE kernel needs 168 registers and loses, 2.01 vs 1.88 ms); ONE_PIXEL the
+// one-pixel kernel with components in order; TWO_PIXEL the two-pixel kernel for either
+// built-in layout; PLAIN_GEOMETRY the all-float32-geometry variant of the DIRBE layout (kept
+// for the precision study).  tails: band tails in the two-pixel kernel (coherent inputs).
+// Models outside the compiled flag sets run the one-pixel kernel with run-time flags.
+cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, int kernel, bool tails, const double* u, int64_t n,
+                           const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   const uint32_t flags = f32_flags(P, layout);
-  // The two-pixel kernel wins where its doubled per-pixel state still leaves enough warps:
-  // measured on GB300 at nside 512, Planck layout 0.79 vs 0.91 ms; for the DIRBE layout it
-  // needs 168 registers and loses (2.01 vs 1.88 ms), so that layout keeps the one-pixel
-  // kernel unless asked (two_pixel_dirbe, a testing hook).
-  // The DIRBE layout runs the component-paired kernel (zl_fwd_dirbe.cuh): ring/feature and
-  // band 1/2 in packed lanes, one pixel per thread.
-  if (!one_pixel && !plain_geometry && flags != kFlagsRuntime) {
+  const bool plain_geometry = kernel == ZL_KERNEL_PLAIN_GEOMETRY;
+  if ((kernel == ZL_KERNEL_AUTO || kernel == ZL_KERNEL_TWO_PIXEL) && flags != kFlagsRuntime) {
     cudaError_t e = cudaErrorNotSupported;
     if (layout == 1)
-      e = g_two_pixel_dirbe ? launch_fwd_f32x2_dirbe(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms)
-                            : launch_fwd_dirbe_cp(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    if (layout == 2) e = launch_fwd_f32x2_planck(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+      e = kernel == ZL_KERNEL_TWO_PIXEL ? launch_fwd_f32x2_dirbe(P, flags, tails, u, n, obs, oc, ot, st, L)
+                                        : launch_fwd_dirbe_cp(P, flags, u, n, obs, oc, ot, st, L);
+    if (layout == 2) e = launch_fwd_f32x2_planck(P, flags, tails, u, n, obs, oc, ot, st, L);
     if (e != cudaErrorNotSupported) return e;
   }
-  if (layout == 1) return launch_fwd_f32_dirbe(P, flags, plain_geometry, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-  if (layout == 2) return launch_fwd_f32_planck(P, flags, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-  return launch_fwd_f32_generic(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+  if (layout == 1) return launch_fwd_f32_dirbe(P, flags, plain_geometry, u, n, obs, oc, ot, st, L);
+  if (layout == 2) return launch_fwd_f32_planck(P, flags, u, n, obs, oc, ot, st, L);
+  return launch_fwd_f32_generic(P, u, n, obs, oc, ot, st, L);
 }
 
 }  // namespace zl

@@ -190,7 +190,8 @@ template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
 __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                       const double* __restrict__ u, int64_t n_pix,
                                                       const ObsArgs OA,
-                                                      double* __restrict__ out_comps, double* __restrict__ out_total) {
+                                                      double* __restrict__ out_comps, double* __restrict__ out_total,
+                                                      const Sched SC) {
   using L = Lay<LAYOUT>;
   using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
   constexpr int NC = L::ncomp();
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
   const int nc = L::generic ? P.n_comps : NC;
   const int nr = P.n_ranges;
 
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
+  ZL_SCHED_LOOP(kSchedAny, SC, n_pix, i) {
     // ---- per-pixel set-up -------------------------------------------------
     PixSetupF32<NC> PS;
     pixel_setup<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, OA, i, PS);
@@ -353,6 +354,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
     }
 
     // ---- outputs: x (stop - start)/2, component order total ----------------
+    const int64_t col = out_col(SC, i);
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s) {
       double tot = 0.0;
@@ -362,45 +364,42 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
         // the compensated sum times (stop - start)/2 in float32 (GB300's FP64 pipe is narrow);
         // the total is the float64 sum of the stored components, so it equals their sum exactly
         const double v = (double)((acc_s[c][s] - acc_c[c][s]) * (hs_c[c].hi + hs_c[c].lo));
-        if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + i] = v;
+        if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + col] = v;
         tot = (c == 0) ? v : __dadd_rn(tot, v);
       }
-      if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
+      if (out_total) out_total[(int64_t)s * n_pix + col] = tot;
     }
   }
+  sched_finish<kSchedAny>(SC);
 }
 
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
 static cudaError_t launch_f32_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
-                                double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                                double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
-  const int64_t blocks_needed = (n + tpb - 1) / tpb;
-  int64_t grid = (int64_t)num_sms * bps;
-  if (grid > blocks_needed) grid = blocks_needed;
-  if (grid < 1) grid = 1;
-  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE, FLAGS><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
+  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE, FLAGS>
+      <<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
   return cudaGetLastError();
 }
 
 // One layout and flag set, every supported number of spectral sets.
 template <uint32_t LAYOUT, uint32_t FLAGS>
 static cudaError_t launch_f32_flags(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
-                                    double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                                    double* ot, cudaStream_t st, const LaunchArgs& L) {
   switch (P.n_spec) {
-    case 1: return launch_f32_t<1, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    case 2: return launch_f32_t<2, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    case 3: return launch_f32_t<3, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    default: return launch_f32_t<4, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 1: return launch_f32_t<1, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, L);
+    case 2: return launch_f32_t<2, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, L);
+    case 3: return launch_f32_t<3, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, L);
+    default: return launch_f32_t<4, LAYOUT, true, FLAGS>(P, u, n, obs, oc, ot, st, L);
   }
 }
 
 // Per-layout launchers (zl_fwd_f32_dirbe.cu, zl_fwd_f32_planck.cu, zl_fwd_f32_generic.cu).
 cudaError_t launch_fwd_f32_dirbe(const KParamsF32& P, uint32_t flags, bool plain_geometry, const double* u, int64_t n,
-                                 const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
-                                 int num_sms);
+                                 const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 cudaError_t launch_fwd_f32_planck(const KParamsF32& P, uint32_t flags, const double* u, int64_t n, const ObsArgs& obs,
-                                  double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
+                                  double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 cudaError_t launch_fwd_f32_generic(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
-                                   double* ot, cudaStream_t st, int tpb, int bps, int num_sms);
+                                   double* ot, cudaStream_t st, const LaunchArgs& L);
 
 }  // namespace zl

@@ -4,8 +4,8 @@
 namespace zl {
 
 cudaError_t launch_fwd_f32_generic(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
-                                   double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
-  return launch_f32_flags<kLayoutGeneric, kFlagsRuntime>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+                                   double* ot, cudaStream_t st, const LaunchArgs& L) {
+  return launch_f32_flags<kLayoutGeneric, kFlagsRuntime>(P, u, n, obs, oc, ot, st, L);
 }
 
 }  // namespace zl

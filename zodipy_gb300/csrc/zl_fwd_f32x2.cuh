@@ -13,9 +13,18 @@
 // operation rounds as its scalar counterpart.  Subtractions a - b are written as
 // fma(b, -1, a), which rounds like a - b.
 //
-// Lanes: thread item t integrates pixels t and t + ceil(n/2), so loads and stores
-// of the [3][n] and [.][n] arrays stay coalesced for any n; for odd n the last item's
-// second lane repeats the first pixel and is not stored.
+// Lanes: the work is cut into tiles of T items (pixel pairs) covering 2T consecutive
+// pixels; item j of tile t integrates pixels 2Tt + j and 2Tt + T + j, so loads and
+// stores of the [3][n] and [.][n] arrays stay coalesced and the two lanes hold
+// neighbours of the input order.  Past the end of the pixels the second lane repeats
+// the first pixel and is not stored.
+//
+// Band tails (TAILS): as in the DIRBE paired kernel (zl_fwd_dirbe.cuh), past the node
+// from which a band's factor e^-(zeta/dzeta)^6 is zero in float32 for both lanes of every
+// thread of the warp, the band adds exactly nothing and a warp-uniform branch skips it.
+// That pays where a warp's pixels are coherent (a HEALPix ring, directions sorted by
+// latitude) and costs the per-pixel estimate and per-node branches where they are not
+// (unsorted random directions), so the caller chooses.
 #pragma once
 
 #include "zl_fwd_f32.cuh"
@@ -23,11 +32,27 @@
 
 namespace zl {
 
-template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS>
+// Band c of a layout: whether a later band reuses its inner-cutoff term 1 - e^-(R/delta_r)^20
+template <uint32_t LAYOUT, uint32_t FLAGS>
+__host__ __device__ constexpr bool t4_shared_later(int c) {
+  for (int j = c + 1; j < Lay<LAYOUT>::ncomp(); ++j)
+    if (Lay<LAYOUT>::type(j) == ZL_BAND && ((FLAGS >> (24 + j)) & 1u) && Lay<LAYOUT>::first_band(j) == c) return true;
+  return false;
+}
+
+// Every band of the layout is centred on the Sun (the band-tail estimate measures from it)
+template <uint32_t LAYOUT, uint32_t FLAGS>
+__host__ __device__ constexpr bool bands_centred() {
+  for (int c = 0; c < Lay<LAYOUT>::ncomp(); ++c)
+    if (Lay<LAYOUT>::type(c) == ZL_BAND && ((FLAGS >> (8 + c)) & 1u)) return false;
+  return true;
+}
+
+template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS, bool TAILS>
 __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ KParamsF32 P,
                                                         const double* __restrict__ u, int64_t n_pix,
                                                         const ObsArgs OA, double* __restrict__ out_comps,
-                                                        double* __restrict__ out_total) {
+                                                        double* __restrict__ out_total, const Sched SC) {
   using L = Lay<LAYOUT>;
   using Fl = KFlags<FLAGS>;
   static_assert(LAYOUT != kLayoutGeneric && !Fl::runtime, "the two-pixel kernel serves the built-in layouts");
@@ -37,10 +62,13 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
   __syncthreads();
 
-  const int64_t half = (n_pix + 1) / 2;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < half; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ia = t;
-    const int64_t ib = t + half < n_pix ? t + half : t;
+  static_assert(!TAILS || bands_centred<LAYOUT, FLAGS>(), "band tails assume bands centred on the Sun");
+  const int64_t TL = sched_tile(SC);
+  const int64_t n_items = ((n_pix + 2 * TL - 1) / (2 * TL)) * TL;
+  ZL_SCHED_LOOP(kSchedAny, SC, n_items, item) {
+    const int64_t ia = item + (item / TL) * TL;  // 2 TL tile + j
+    if (ia >= n_pix) continue;
+    const int64_t ib = ia + TL < n_pix ? ia + TL : ia;
 
     // ---- per-pixel set-up, one lane at a time, then packed ---------------
     ff2 hs[NC], mh[NC], z1[NC], z0[NC], wm[NC], wa[NC], wb[NC];
@@ -68,6 +96,27 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
       }
       b2h = make_float2(A.b2h, B.b2h);
       bperp = make_float2(A.bperp, B.bperp);
+    }
+
+    // band tails: kt[c] = first node from which band c is zero for the whole warp; kt4[c] = first
+    // node from which its inner-cutoff term is needed by no band of the warp
+    int kt[NC], kt4[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) kt[c] = kt4[c] = P.n_nodes;
+    if (TAILS) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (L::type(c) == ZL_BAND) {
+          const float ta = band_zero_tail(z1[c].hi.x, z0[c].hi.x, hs[c].hi.x, mh[c].hi.x, b2h.x, P.comp[c].c[1]);
+          const float tb = band_zero_tail(z1[c].hi.y, z0[c].hi.y, hs[c].hi.y, mh[c].hi.y, b2h.y, P.comp[c].c[1]);
+          kt[c] = kt4[c] = warp_tail_index(P, fmaxf(ta, tb));
+        }
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (L::type(c) == ZL_BAND && Fl::share_first(c)) {
+          const int f = L::first_band(c);
+          kt4[f] = max(kt4[f], kt[c]);
+        }
     }
 
     // quadrature sums: plain float32 over blocks of kSumBlock nodes, Kahan-compensated across blocks
@@ -137,6 +186,24 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
           const float2 gg = ex2_2(mul2(bc2(C.c[3]), lg2_2(g)));
           dens = ex2_2(fma2(bc2(-C.c[1]), lg2Rc, mul2(bc2(-C.c[2]), gg)));
         } else if (type == ZL_BAND) {  // number_density.py:99-110
+          if (TAILS && k >= kt[c]) {
+            // zero for every pixel of the warp from here on; a later band may still need the
+            // inner-cutoff term
+            if (t4_shared_later<LAYOUT, FLAGS>(c) && k < kt4[c]) {
+              const float2 q = mul2(Rc2, bc2(C.c[4]));
+              const float2 q2 = mul2(q, q), q4 = mul2(q2, q2), q8 = mul2(q4, q4);
+              const float2 y = mul2(q8, q2);
+              const float2 ny = mul2(y, bc2(-1.f));
+              float2 ser = fma2(ny, bc2(1.f / 720.f), bc2(1.f / 120.f));
+              ser = fma2(ny, ser, bc2(1.f / 24.f));
+              ser = fma2(ny, ser, bc2(1.f / 6.f));
+              ser = fma2(ny, ser, bc2(0.5f));
+              ser = mul2(y, fma2(ny, ser, bc2(1.f)));
+              const float2 alt = sub2(bc2(1.f), ex2_2(mul2(bc2(-kLog2e), y)));
+              t4s[c] = make_float2(y.x < 0.25f ? ser.x : alt.x, y.y < 0.25f ? ser.y : alt.y);
+            }
+            continue;
+          }
           const float2 zz = mul2(mul2(abs2(Z), rcinv), bc2(C.c[1]));
           const float2 z2 = mul2(zz, zz);
           const float2 t2 = ex2_2(mul2(bc2(-kLog2e), mul2(mul2(z2, z2), z2)));
@@ -201,7 +268,7 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
 #pragma unroll
     for (int lane = 0; lane < 2; ++lane) {
       if (lane == 1 && ib == ia) break;
-      const int64_t i = lane ? ib : ia;
+      const int64_t i = out_col(SC, lane ? ib : ia);
 #pragma unroll
       for (int s = 0; s < NSPEC; ++s) {
         double tot = 0.0;
@@ -220,39 +287,37 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
       }
     }
   }
+  sched_finish<kSchedAny>(SC);
 }
 
-template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS>
+template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS, bool TAILS>
 static cudaError_t launch_f32x2_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
-                                  double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                                  double* ot, cudaStream_t st, const LaunchArgs& L) {
   const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
-  const int64_t items = (n + 1) / 2;
-  const int64_t blocks_needed = (items + tpb - 1) / tpb;
-  int64_t grid = (int64_t)num_sms * bps;
-  if (grid > blocks_needed) grid = blocks_needed;
-  if (grid < 1) grid = 1;
-  fwd_f32x2_kernel<NSPEC, LAYOUT, FLAGS><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
+  const int64_t T = L.sched.queue ? L.sched.tile : L.tpb;
+  const int64_t items = ((n + 2 * T - 1) / (2 * T)) * T;
+  fwd_f32x2_kernel<NSPEC, LAYOUT, FLAGS, TAILS>
+      <<<(unsigned)fwd_grid(L, items), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
   return cudaGetLastError();
 }
 
-template <uint32_t LAYOUT, uint32_t FLAGS>
+template <uint32_t LAYOUT, uint32_t FLAGS, bool TAILS>
 static cudaError_t launch_f32x2_flags(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
-                                      double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                                      double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   switch (P.n_spec) {
-    case 1: return launch_f32x2_t<1, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    case 2: return launch_f32x2_t<2, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    case 3: return launch_f32x2_t<3, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    default: return launch_f32x2_t<4, LAYOUT, FLAGS>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 1: return launch_f32x2_t<1, LAYOUT, FLAGS, TAILS>(P, u, n, obs, oc, ot, st, L);
+    case 2: return launch_f32x2_t<2, LAYOUT, FLAGS, TAILS>(P, u, n, obs, oc, ot, st, L);
+    case 3: return launch_f32x2_t<3, LAYOUT, FLAGS, TAILS>(P, u, n, obs, oc, ot, st, L);
+    default: return launch_f32x2_t<4, LAYOUT, FLAGS, TAILS>(P, u, n, obs, oc, ot, st, L);
   }
 }
 
 // Two-pixel launchers of the built-in layouts (zl_fwd_f32x2_dirbe.cu, zl_fwd_f32x2_planck.cu);
-// they return cudaErrorNotSupported for a flag set they are not compiled for.
-cudaError_t launch_fwd_f32x2_dirbe(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
-                                   const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
-                                   int num_sms);
-cudaError_t launch_fwd_f32x2_planck(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
-                                    const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
-                                    int num_sms);
+// they return cudaErrorNotSupported for a flag set they are not compiled for.  tails: skip the
+// bands' zero tails (coherent inputs).
+cudaError_t launch_fwd_f32x2_dirbe(const KParamsF32& P, uint32_t flags, bool tails, const double* u, int64_t n,
+                                   const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
+cudaError_t launch_fwd_f32x2_planck(const KParamsF32& P, uint32_t flags, bool tails, const double* u, int64_t n,
+                                    const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 
 }  // namespace zl

@@ -3,13 +3,14 @@
 
 namespace zl {
 
-cudaError_t launch_fwd_f32x2_dirbe(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
-                                   const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
-                                   int num_sms) {
+cudaError_t launch_fwd_f32x2_dirbe(const KParamsF32& P, uint32_t flags, bool tails, const double* u, int64_t n,
+                                   const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   if (flags == kFlagsKelsall)
-    return launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    return tails ? launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall, true>(P, u, n, obs, oc, ot, st, L)
+                 : launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall, false>(P, u, n, obs, oc, ot, st, L);
   if (flags == (kFlagsKelsall | 2u))
-    return launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall | 2u>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    return tails ? launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall | 2u, true>(P, u, n, obs, oc, ot, st, L)
+                 : launch_f32x2_flags<kLayoutDirbe, kFlagsKelsall | 2u, false>(P, u, n, obs, oc, ot, st, L);
   return cudaErrorNotSupported;
 }
 

@@ -3,11 +3,11 @@
 
 namespace zl {
 
-cudaError_t launch_fwd_f32x2_planck(const KParamsF32& P, uint32_t flags, const double* u, int64_t n,
-                                    const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, int tpb, int bps,
-                                    int num_sms) {
+cudaError_t launch_fwd_f32x2_planck(const KParamsF32& P, uint32_t flags, bool tails, const double* u, int64_t n,
+                                    const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   if (flags == kFlagsKelsall)
-    return launch_f32x2_flags<kLayoutPlanck, kFlagsKelsall>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    return tails ? launch_f32x2_flags<kLayoutPlanck, kFlagsKelsall, true>(P, u, n, obs, oc, ot, st, L)
+                 : launch_f32x2_flags<kLayoutPlanck, kFlagsKelsall, false>(P, u, n, obs, oc, ot, st, L);
   return cudaErrorNotSupported;
 }
 

@@ -144,7 +144,8 @@ template <int NSPEC>
 __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KParamsF64 P,
                                                       const double* __restrict__ u, int64_t n_pix,
                                                       const ObsArgs OA,
-                                                      double* __restrict__ out_comps, double* __restrict__ out_total) {
+                                                      double* __restrict__ out_comps, double* __restrict__ out_total,
+                                                      const Sched SC) {
   extern __shared__ double sm[];
   const int nT = P.m.n_temps;
   double* xp = sm;                  // [nT]
@@ -164,7 +165,7 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
   const int nc = P.m.n_comps;
   const int nr = P.m.n_ranges;
 
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += (int64_t)gridDim.x * blockDim.x) {
+  ZL_SCHED_LOOP(kSchedAny, SC, n_pix, i) {
     const double ux = u[i], uy = u[n_pix + i], uz = u[2 * n_pix + i];
     const PixObs O = pixel_observer(OA, i, n_pix);
     const double ox = O.ox, oy = O.oy, oz = O.oz;
@@ -252,29 +253,27 @@ __global__ void __launch_bounds__(128) fwd_f64_kernel(const __grid_constant__ KP
       }
     }
 
+    const int64_t col = out_col(SC, i);
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s) {
       double tot = 0.0;
 #pragma unroll
       for (int c = 0; c < ZL_MAX_COMPS; ++c) {
         if (c >= nc) break;
-        if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + i] = acc[c][s];
+        if (out_comps) out_comps[((int64_t)s * nc + c) * n_pix + col] = acc[c][s];
         tot = (c == 0) ? acc[c][s] : tot + acc[c][s];
       }
-      if (out_total) out_total[(int64_t)s * n_pix + i] = tot;
+      if (out_total) out_total[(int64_t)s * n_pix + col] = tot;
     }
   }
+  sched_finish<kSchedAny>(SC);
 }
 
 template <int NSPEC>
 static cudaError_t launch_f64_t(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
-                                double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                                double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   const size_t smem = sizeof(double) * P.m.n_temps * (1 + 2 * NSPEC);
-  int64_t blocks_needed = (n + tpb - 1) / tpb;
-  int64_t grid = (int64_t)num_sms * bps;
-  if (grid > blocks_needed) grid = blocks_needed;
-  if (grid < 1) grid = 1;
-  fwd_f64_kernel<NSPEC><<<(unsigned)grid, tpb, smem, st>>>(P, u, n, obs, oc, ot);
+  fwd_f64_kernel<NSPEC><<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
   return cudaGetLastError();
 }
 
@@ -307,12 +306,12 @@ cudaError_t launch_density_grid(const ZlModel& M, const double* x, int nx, const
 }
 
 cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
-                           double* oc, double* ot, cudaStream_t st, int tpb, int bps, int num_sms) {
+                           double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   switch (P.m.n_spec) {
-    case 1: return launch_f64_t<1>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    case 2: return launch_f64_t<2>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    case 3: return launch_f64_t<3>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
-    default: return launch_f64_t<4>(P, u, n, obs, oc, ot, st, tpb, bps, num_sms);
+    case 1: return launch_f64_t<1>(P, u, n, obs, oc, ot, st, L);
+    case 2: return launch_f64_t<2>(P, u, n, obs, oc, ot, st, L);
+    case 3: return launch_f64_t<3>(P, u, n, obs, oc, ot, st, L);
+    default: return launch_f64_t<4>(P, u, n, obs, oc, ot, st, L);
   }
 }
 

@@ -56,8 +56,10 @@ def forward(
     out_comps=None,
     out_total=None,
     stream: int | None = None,
+    launch: _lib.ZlLaunch | None = None,
 ):
-    """Run ``zl_forward``; returns (comps [n_spec, C, N] or None, total [n_spec, N] or None)."""
+    """Run ``zl_forward`` (``zl_forward_ex`` when ``launch`` options are given); returns
+    (comps [n_spec, C, N] or None, total [n_spec, N] or None)."""
     torch = _torch()
     if u_dev.dtype != torch.float64 or not u_dev.is_cuda or u_dev.dim() != 2 or u_dev.shape[0] != 3:
         raise ValueError("unit vectors must be a float64 CUDA tensor of shape (3, N)")
@@ -70,7 +72,7 @@ def forward(
     if want_total and out_total is None:
         out_total = torch.empty((ns, n), dtype=torch.float64, device=dev)
     lib = _lib.load()
-    rc = lib.zl_forward(
+    rc = lib.zl_forward_ex(
         ctypes.byref(zl_model),
         ctypes.c_void_p(u_dev.data_ptr()),
         n,
@@ -79,10 +81,33 @@ def forward(
         precision_code(precision),
         ctypes.c_void_p(out_comps.data_ptr() if out_comps is not None else 0),
         ctypes.c_void_p(out_total.data_ptr() if out_total is not None else 0),
+        ctypes.byref(launch) if launch is not None else None,
         ctypes.c_void_p(stream if stream is not None else current_stream_handle(dev)),
     )
     _lib.check(rc, "zl_forward")
     return (out_comps if want_comps else None), (out_total if want_total else None)
+
+
+def launch_options(threads_per_block: int = 0, blocks_per_sm: int = 0, kernel: int = _lib.ZL_KERNEL_AUTO,
+                   band_tails: bool = False, tile: int = 0, queue=None, out_index=None) -> _lib.ZlLaunch:
+    """A ``ZlLaunch`` for one call; ``queue`` (two int32 words, zero) and ``out_index`` (int64, a
+    permutation of the call's pixel indices) are CUDA tensors.  The struct holds references to
+    both, so they stay allocated as long as it does (it carries only their addresses to the
+    library)."""
+    if out_index is not None and (out_index.dtype != _torch().int64 or not out_index.is_cuda):
+        raise ValueError("out_index must be an int64 CUDA tensor")
+    if queue is not None and (queue.numel() < 2 or queue.element_size() != 4 or not queue.is_cuda):
+        raise ValueError("queue must be a CUDA tensor of two 32-bit words")
+    opt = _lib.ZlLaunch()
+    opt._keep = (queue, out_index)
+    opt.threads_per_block = int(threads_per_block)
+    opt.blocks_per_sm = int(blocks_per_sm)
+    opt.kernel = int(kernel)
+    opt.band_tails = 1 if band_tails else 0
+    opt.tile = int(tile)
+    opt.queue_dev = queue.data_ptr() if queue is not None else None
+    opt.out_index_dev = out_index.data_ptr() if out_index is not None else None
+    return opt
 
 
 def grad_count(zl_model: _lib.ZlModel) -> int:
@@ -110,8 +135,10 @@ def backward(
     grad_out=None,
     workspace=None,
     stream: int | None = None,
+    launch: _lib.ZlLaunch | None = None,
 ):
-    """Run ``zl_backward``: gradient (float64 CUDA tensor) of the loss w.r.t. the parameter vector."""
+    """Run ``zl_backward`` (``zl_backward_ex`` with ``launch`` options): gradient (float64 CUDA
+    tensor) of the loss w.r.t. the parameter vector."""
     torch = _torch()
     if (g_comps is None) == (g_total is None):
         raise ValueError("pass exactly one of g_comps (n_spec, C, N) or g_total (n_spec, N)")
@@ -127,7 +154,7 @@ def backward(
     need = backward_workspace_bytes(zl_model, n)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
         workspace = torch.empty(max(need, 8), dtype=torch.uint8, device=dev)
-    rc = _lib.load().zl_backward(
+    rc = _lib.load().zl_backward_ex(
         ctypes.byref(zl_model),
         ctypes.c_void_p(u_dev.data_ptr()),
         n,
@@ -138,6 +165,7 @@ def backward(
         ctypes.c_void_p(grad_out.data_ptr()),
         ctypes.c_void_p(workspace.data_ptr()),
         workspace.numel() * workspace.element_size(),
+        ctypes.byref(launch) if launch is not None else None,
         ctypes.c_void_p(stream if stream is not None else current_stream_handle(dev)),
     )
     _lib.check(rc, "zl_backward")
