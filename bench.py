@@ -552,7 +552,7 @@ def main():
         nb = int(bcounts.sum())
         bu = random_directions_device(nb, seed=2025, device=dev)
         ev = BatchEvaluator(pm.zl_model, bu, bobs, bcounts, workload(args.nside)[2], precision="float32")
-        tpb, bps_b, tile_b, _ = ev.autotune(sample=1 << 21, reps=2, use_cache=False)
+        tpb, bps_b, tile_b, tails_b, _ = ev.autotune(sample=1 << 21, reps=2, use_cache=False)
         ev.capture()
         for _ in range(2):
             ev.replay()
@@ -581,7 +581,7 @@ def main():
             "ms_per_launch": bms,
             "los_per_s": nb / (bms * 1e-3),
             "autotuned_launch": {"threads_per_block": tpb, "blocks_per_sm": bps_b, "queue_tile": tile_b,
-                                 "sorted_by_latitude": ev.sorted, "band_tails": ev.sorted},
+                                 "sorted_by_latitude": ev.sorted, "band_tails": tails_b},
             "rel_err_fp32_vs_fp64": err_b,
         }
         del ev, bu

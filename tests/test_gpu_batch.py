@@ -72,10 +72,10 @@ def test_graph_replay_equals_eager_and_launch_shape_does_not_matter(lib):
 
     model, obs, counts, uu, earth = _setup(n_obs=9, lo=2000, hi=9000)
     plain = BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32", sort=False)
-    plain.set_launch(64, 0, 0)
+    plain.set_launch(64, 0, 0, False)
     ref = plain.run().clone()
     ev = BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
-    for launch in ((64, 3, 64), (128, 0, 0), (128, 8, 512)):
+    for launch in ((64, 3, 64, True), (128, 0, 0, False), (128, 8, 512, True), (96, 0, 0, True)):
         ev.set_launch(*launch)
         np.testing.assert_array_equal(ev.run().cpu().numpy(), ref.cpu().numpy())
     ev.capture()
@@ -111,16 +111,16 @@ def test_tuning_one_evaluator_leaves_other_calls_alone(lib, tmp_path, monkeypatc
     monkeypatch.setattr(batch, "CACHE_PATH", str(tmp_path / "tune.json"))
     model, obs, counts, uu, earth = _setup(n_obs=4, lo=20000, hi=40000)
     other = batch.BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
-    other.set_launch(96, 0, 0)
+    other.set_launch(96, 0, 0, True)
     before = other.run().cpu().numpy().copy()
     probe = uu[:, :500]
     m_before = model.evaluate_xyz(probe, obs[:, 0], earth, return_comps=True, precision="float32").cpu().numpy()
     ev = batch.BatchEvaluator(model.zl_model, uu, obs, counts, earth, precision="float32")
-    tpb, bps, tile, ms = ev.autotune(sample=1 << 16, reps=1)
-    assert (tpb, bps, tile) in batch.STATIC_CHOICES + batch.QUEUE_CHOICES and ms > 0
-    assert ev.launch == (tpb, bps, tile) and other.launch == (96, 0, 0)
+    tpb, bps, tile, tails, ms = ev.autotune(sample=1 << 16, reps=1)
+    assert (tpb, bps, tile, tails) in batch.STATIC_CHOICES + batch.QUEUE_CHOICES and ms > 0
+    assert ev.launch == (tpb, bps, tile, tails) and other.launch == (96, 0, 0, True)
     again = ev.autotune(sample=1 << 16, reps=1)  # from the cache
-    assert tuple(again[:3]) == (tpb, bps, tile)
+    assert tuple(again[:4]) == (tpb, bps, tile, tails)
     np.testing.assert_array_equal(other.run().cpu().numpy(), before)
     m_after = model.evaluate_xyz(probe, obs[:, 0], earth, return_comps=True, precision="float32").cpu().numpy()
     np.testing.assert_array_equal(m_after, m_before)

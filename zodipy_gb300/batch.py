@@ -34,10 +34,13 @@ import torch
 
 from . import _lib, engine, packing
 
-# (threads per block, blocks per SM, tile in items); blocks per SM 0 with tile 0 = the static
-# one-block-per-tile launch
-STATIC_CHOICES = tuple((tpb, 0, 0) for tpb in (64, 96, 128))
-QUEUE_CHOICES = tuple((tpb, bps, tpb * k) for tpb in (64, 128) for bps in (2, 4, 6, 8, 16) for k in (1, 2, 4, 8))
+# (threads per block, blocks per SM, tile in items, band tails); blocks per SM 0 with tile 0 = the
+# static one-block-per-tile launch.  Band tails (skipping the dust bands' zero terms for a whole
+# warp) pay only where a warp's lines of sight are alike, and cost a test per node where they are
+# not, so the tuner times both on a sorted batch.
+STATIC_CHOICES = tuple((tpb, 0, 0, tails) for tpb in (64, 96, 128) for tails in (False, True))
+QUEUE_CHOICES = tuple((tpb, bps, tpb * k, tails) for tpb in (64, 128) for bps in (2, 4, 6, 8, 16) for k in (1, 2, 4, 8)
+                      for tails in (False, True))
 CACHE_PATH = os.environ.get("ZODIGB_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "zodigb_tune.json"))
 
 
@@ -89,11 +92,11 @@ class BatchEvaluator:
         self.comps = torch.empty((ns, nc, self.n), dtype=torch.float64, device=dev) if comps else None
         self.queue = torch.zeros(2, dtype=torch.int32, device=dev)
         self.graph = None
-        self.set_launch(128, 8, 256)
+        self.set_launch(128, 8, 256, False)
 
     # -- execution -----------------------------------------------------------
-    def _options(self, tpb: int, bps: int, tile: int) -> _lib.ZlLaunch:
-        return engine.launch_options(threads_per_block=tpb, blocks_per_sm=bps, band_tails=self.sorted, tile=tile,
+    def _options(self, tpb: int, bps: int, tile: int, tails: bool) -> _lib.ZlLaunch:
+        return engine.launch_options(threads_per_block=tpb, blocks_per_sm=bps, band_tails=tails, tile=tile,
                                      queue=self.queue if tile > 0 else None, out_index=self.order)
 
     def run(self, stream=None, n: int | None = None):
@@ -114,9 +117,9 @@ class BatchEvaluator:
         )
         return self.total
 
-    def set_launch(self, tpb: int, bps: int, tile: int = 0) -> None:
+    def set_launch(self, tpb: int, bps: int, tile: int = 0, tails: bool = False) -> None:
         """This evaluator's launch shape (other evaluators and models are not affected)."""
-        self.launch = (int(tpb), int(bps), int(tile))
+        self.launch = (int(tpb), int(bps), int(tile), bool(tails))
         self.launch_opt = self._options(*self.launch)
         self.graph = None
 
@@ -143,26 +146,30 @@ class BatchEvaluator:
     def _key(self) -> str:
         props = torch.cuda.get_device_properties(self.u.device)
         comp = "".join(str(self.zl.comp[c].type) for c in range(self.zl.n_comps))
-        return (f"v3|{props.name}|sm{props.multi_processor_count}|p{self.prec}|c{comp}|s{self.zl.n_spec}"
+        return (f"v4|{props.name}|sm{props.multi_processor_count}|p{self.prec}|c{comp}|s{self.zl.n_spec}"
                 f"|k{self.zl.n_nodes}|sorted{int(self.sorted)}")
 
     def autotune(self, sample: int | None = 1 << 21, reps: int = 3, use_cache: bool = True):
-        """Time every candidate (threads per block, blocks per SM, tile) on a sample; keep the fastest.
+        """Time every candidate (threads per block, blocks per SM, tile, band tails) on a sample;
+        keep the fastest.
 
         Candidates: the static one-block-per-tile launch and work-queue launches of several
-        tile sizes and grid caps.  The sample is the first ``sample`` pixels of the evaluation
+        tile sizes and grid caps, each with and without band tails (without only, for an
+        unsorted batch, whose warps are too mixed for them).  The sample is the first ``sample`` pixels of the evaluation
         order (whole observers, whose directions span every latitude).  Results are cached per
-        GPU and workload signature.  Returns (tpb, bps, tile, ms_per_launch_on_sample).
+        GPU and workload signature.  Returns (tpb, bps, tile, tails, ms_per_launch_on_sample).
         """
         key = self._key()
         cache = _load_cache() if use_cache else {}
         if key in cache:
-            tpb, bps, tile, ms = cache[key]
-            self.set_launch(tpb, bps, tile)
-            return tpb, bps, tile, ms
+            tpb, bps, tile, tails, ms = cache[key]
+            self.set_launch(tpb, bps, tile, tails)
+            return tpb, bps, tile, bool(tails), ms
         n = self.n if sample is None else min(self.n, int(sample))
         best = None
         for cand in STATIC_CHOICES + QUEUE_CHOICES:
+            if cand[3] and not self.sorted:
+                continue
             self.set_launch(*cand)
             self.run(n=n)
             torch.cuda.synchronize()
@@ -175,9 +182,9 @@ class BatchEvaluator:
                 ts.append((a, b))
             torch.cuda.synchronize()
             ms = min(a.elapsed_time(b) for a, b in ts)
-            if best is None or ms < best[3]:
+            if best is None or ms < best[4]:
                 best = (*cand, ms)
-        self.set_launch(*best[:3])
+        self.set_launch(*best[:4])
         if use_cache:
             cache[key] = list(best)
             _save_cache(cache)

@@ -96,8 +96,9 @@ __device__ __forceinline__ RrmTerms rrm_terms(const float* q, float r2in, float 
   const float s = fminf(fmaxf(Z * rcinv, -1.f), 1.f);
   const float beta = asinf(s);
   const float cb = sqrtf(fmaxf(1.f - s * s, 0.f));
-  // d beta / d Z and d beta / d Rc at fixed Rc, Z
-  const float icb = cb > 0.f ? 1.f / cb : 0.f;
+  // d beta / d Z and d beta / d Rc at fixed Rc, Z; cos(beta) floored at 1e-6 so that a node
+  // on the axis (|Z| = Rc, where the derivative has no finite value) gives large but finite terms
+  const float icb = 1.f / fmaxf(cb, 1e-6f);
   const float dbZ = rcinv * icb;
   const float dbR = -s * rcinv * icb;
   const float lnR = __logf(Rc);
@@ -119,7 +120,7 @@ __device__ __forceinline__ RrmTerms rrm_terms(const float* q, float r2in, float 
     if (TYPE == ZL_FAN) {
       const float Q = q[2];
       lnf += Q * __logf(fmaxf(cb, 1e-30f));
-      Gb += -Q * (cb > 0.f ? s * icb : 0.f);  // d/d beta of Q ln cos beta = -Q tan beta
+      Gb += -Q * s * icb;  // d/d beta of Q ln cos beta = -Q tan beta
     }
     const float amp = TYPE == ZL_FAN ? 1.f : q[3];
     t.n = amp * __expf(-gamma * lnR + lnf);
@@ -160,7 +161,9 @@ __device__ __forceinline__ RrmTerms rrm_terms(const float* q, float r2in, float 
   const float e1 = __expf(-0.5f * a * a), e2 = __expf(-0.5f * b * b);
   const float f = e1 + e2;
   t.n = A * radial * f;
-  const float inf = f > 0.f ? 1.f / f : 0.f;
+  // 1/f where f is a normal float32 (e1 and e2 are both below f, so each ratio stays bounded);
+  // where both Gaussians have underflowed the density and its derivatives are zero
+  const float inf = f > 1e-30f ? 1.f / f : 0.f;
   const float Gb = -(a * e1 + b * e2) / sbb * inf * kRad2Deg;  // d ln f / d beta [rad]
   t.GR = -gamma * rcinv + Gb * dbR;
   t.GZ = Gb * dbZ;

@@ -425,6 +425,10 @@ __device__ __forceinline__ int64_t sched_next(const Sched& S, int64_t i, int64_t
     if (::zl::sched_queued<MODE>(S) && i >= (n_items)) continue;                                         \
     else
 
+// First item of the tile that item i of a ZL_SCHED_LOOP belongs to (inside the loop only): the
+// fetched tile's base with the queue, else the block's share of this grid-stride pass.
+#define ZL_SCHED_TILE_BASE(MODE, S, i) (::zl::sched_queued<MODE>(S) ? _zl_tb : (i) - (int64_t)threadIdx.x)
+
 // Host side of a forward launch: block shape, grid sizing and the schedule.
 struct LaunchArgs {
   int tpb;      // threads per block

@@ -51,7 +51,8 @@ __host__ __device__ constexpr bool bands_centred() {
 template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS, bool TAILS>
 __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ KParamsF32 P,
                                                         const double* __restrict__ u, int64_t n_pix,
-                                                        const ObsArgs OA, double* __restrict__ out_comps,
+                                                        int64_t n_items, const ObsArgs OA,
+                                                        double* __restrict__ out_comps,
                                                         double* __restrict__ out_total, const Sched SC) {
   using L = Lay<LAYOUT>;
   using Fl = KFlags<FLAGS>;
@@ -63,10 +64,11 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
   __syncthreads();
 
   static_assert(!TAILS || bands_centred<LAYOUT, FLAGS>(), "band tails assume bands centred on the Sun");
+  // n_items = TL x the number of 2 TL-pixel tiles (TL: the schedule's tile): item j of tile k
+  // evaluates pixels 2 TL k + j and 2 TL k + j + TL
   const int64_t TL = sched_tile(SC);
-  const int64_t n_items = ((n_pix + 2 * TL - 1) / (2 * TL)) * TL;
   ZL_SCHED_LOOP(kSchedAny, SC, n_items, item) {
-    const int64_t ia = item + (item / TL) * TL;  // 2 TL tile + j
+    const int64_t ia = item + ZL_SCHED_TILE_BASE(kSchedAny, SC, item);
     if (ia >= n_pix) continue;
     const int64_t ib = ia + TL < n_pix ? ia + TL : ia;
 
@@ -297,7 +299,7 @@ static cudaError_t launch_f32x2_t(const KParamsF32& P, const double* u, int64_t 
   const int64_t T = L.sched.queue ? L.sched.tile : L.tpb;
   const int64_t items = ((n + 2 * T - 1) / (2 * T)) * T;
   fwd_f32x2_kernel<NSPEC, LAYOUT, FLAGS, TAILS>
-      <<<(unsigned)fwd_grid(L, items), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
+      <<<(unsigned)fwd_grid(L, items), L.tpb, smem, st>>>(P, u, n, items, obs, oc, ot, L.sched);
   return cudaGetLastError();
 }
 
