@@ -137,12 +137,17 @@ typedef struct ZlObserver {
   uint32_t reserved;
 } ZlObserver;
 
-/* Which float32 kernel serves a call (ZlLaunch.kernel). */
+/* Which kernel serves a call (ZlLaunch.kernel).  float32: AUTO, ONE_PIXEL, TWO_PIXEL,
+ * PLAIN_GEOMETRY; float64 forward: AUTO (= ONE_PIXEL) or WARP_PER_PIXEL; adjoint: AUTO or
+ * ONE_PIXEL.  Any other pairing is refused with ZL_ERR_ARG. */
 enum {
-  ZL_KERNEL_AUTO = 0,          /* the fastest measured kernel for the model's layout */
-  ZL_KERNEL_ONE_PIXEL = 1,     /* one pixel per thread, components in order (forward and adjoint) */
-  ZL_KERNEL_TWO_PIXEL = 2,     /* forward: two pixels per thread on packed float32 (built-in layouts) */
-  ZL_KERNEL_PLAIN_GEOMETRY = 3 /* forward, DIRBE layout: all-float32 geometry (a precision study) */
+  ZL_KERNEL_AUTO = 0,           /* the fastest measured kernel for the model's layout */
+  ZL_KERNEL_ONE_PIXEL = 1,      /* one pixel per thread, components in order (forward and adjoint) */
+  ZL_KERNEL_TWO_PIXEL = 2,      /* float32 forward: two pixels per thread on packed float32 (built-in layouts) */
+  ZL_KERNEL_PLAIN_GEOMETRY = 3, /* float32 forward, DIRBE layout: all-float32 geometry (a precision study) */
+  ZL_KERNEL_WARP_PER_PIXEL = 4  /* float64 forward: one warp per pixel, nodes across the lanes, shuffle
+                                   sums (no work queue); the sum over nodes is associated differently
+                                   from the reference's sequential sum (last bits) */
 };
 
 /* Launch options of one call (NULL = the defaults).  The library keeps no launch

@@ -20,16 +20,20 @@ LIB_PATH = os.path.join(PKG_DIR, "libzodigb.so")
 SOURCES = [
     "zl_api.cu",
     "zl_fwd_f64.cu",
+    "zl_fwd_f64_warp.cu",
     "zl_fwd_f32.cu",
     "zl_fwd_f32_dirbe.cu",
     "zl_fwd_f32_planck.cu",
     "zl_fwd_f32_generic.cu",
     "zl_fwd_f32x2_dirbe.cu",
+    "zl_fwd_f32x2_dirbe_scat.cu",
     "zl_fwd_f32x2_planck.cu",
     "zl_fwd_dirbe_cp.cu",
     "zl_bwd_f32.cu",
     "zl_bwd_f32_dirbe.cu",
+    "zl_bwd_f32_dirbe34.cu",
     "zl_bwd_dirbe_cp.cu",
+    "zl_bwd_dirbe_cp34.cu",
     "zl_bwd_f32_planck.cu",
     "zl_bwd_rrm.cu",
     "zl_diag.cu",

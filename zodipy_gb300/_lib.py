@@ -25,7 +25,7 @@ ZL_KELSALL, ZL_RRM = 0, 1
 ZL_SEMB_L2_SCRATCH = 1024
 ZL_PREC_F64, ZL_PREC_F32 = 0, 1
 ZL_OK, ZL_ERR_ARG, ZL_ERR_CUDA, ZL_ERR_MODEL, ZL_ERR_SPACE = 0, -1, -2, -3, -4
-ZL_KERNEL_AUTO, ZL_KERNEL_ONE_PIXEL, ZL_KERNEL_TWO_PIXEL, ZL_KERNEL_PLAIN_GEOMETRY = 0, 1, 2, 3
+ZL_KERNEL_AUTO, ZL_KERNEL_ONE_PIXEL, ZL_KERNEL_TWO_PIXEL, ZL_KERNEL_PLAIN_GEOMETRY, ZL_KERNEL_WARP_PER_PIXEL = 0, 1, 2, 3, 4
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
 

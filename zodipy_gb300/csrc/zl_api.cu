@@ -11,7 +11,7 @@
 #include "zl_common.cuh"
 
 namespace zl {
-cudaError_t launch_fwd_f64(const KParamsF64& P, const double* u, int64_t n, const ObsArgs& obs,
+cudaError_t launch_fwd_f64(const KParamsF64& P, bool warp, const double* u, int64_t n, const ObsArgs& obs,
                            double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, int kernel, bool tails, const double* u, int64_t n,
                            const ObsArgs& obs, double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
@@ -168,7 +168,7 @@ int launch_options(const ZlLaunch* in, ZlLaunch* out) {
     return fail(ZL_ERR_ARG, "threads_per_block %d not in {32..128 step 32}", d.threads_per_block);
   if (d.blocks_per_sm < 0 || d.blocks_per_sm > kBpsOnePixelPerThread)
     return fail(ZL_ERR_ARG, "blocks_per_sm %d out of [0,%d]", d.blocks_per_sm, kBpsOnePixelPerThread);
-  if (d.kernel < ZL_KERNEL_AUTO || d.kernel > ZL_KERNEL_PLAIN_GEOMETRY) return fail(ZL_ERR_ARG, "bad kernel %d", d.kernel);
+  if (d.kernel < ZL_KERNEL_AUTO || d.kernel > ZL_KERNEL_WARP_PER_PIXEL) return fail(ZL_ERR_ARG, "bad kernel %d", d.kernel);
   if (d.band_tails != 0 && d.band_tails != 1) return fail(ZL_ERR_ARG, "band_tails %d not 0 or 1", d.band_tails);
   if (d.tile < 0 || d.tile > kMaxQueueTile) return fail(ZL_ERR_ARG, "tile %d out of [0,%d]", d.tile, kMaxQueueTile);
   if (d.tile > 0 && (d.tile % d.threads_per_block))
@@ -421,8 +421,12 @@ int forward_impl(const ZlModel* model, const double* u, int64_t n_pix, const Obs
   if (precision == ZL_PREC_F64) {
     static thread_local KParamsF64 P;
     build_f64(*model, &P);
+    const bool warp = opt.kernel == ZL_KERNEL_WARP_PER_PIXEL;
+    if (opt.kernel != ZL_KERNEL_AUTO && opt.kernel != ZL_KERNEL_ONE_PIXEL && !warp)
+      return fail(ZL_ERR_ARG, "the float64 forward has no kernel %d", opt.kernel);
+    if (warp && opt.queue_dev) return fail(ZL_ERR_ARG, "the warp-per-pixel kernel takes no work queue");
     if (!L.bps) L.bps = 8;
-    e = launch_fwd_f64(P, u, n_pix, OA, out_comps, out_total, st, L);
+    e = launch_fwd_f64(P, warp, u, n_pix, OA, out_comps, out_total, st, L);
   } else {
     static thread_local KParamsF32 P;
     build_f32(*model, &P);
@@ -430,6 +434,7 @@ int forward_impl(const ZlModel* model, const double* u, int64_t n_pix, const Obs
     // cost different amounts (a warp whose pixels are all past a band's zero tail skips it), so
     // many short blocks balance the SMs better than a few long-running ones (DIRBE 25 um at nside
     // 512: 1.48 ms with 8 blocks per SM, 1.33 ms); a queued launch defaults to 8 blocks per SM.
+    if (opt.kernel == ZL_KERNEL_WARP_PER_PIXEL) return fail(ZL_ERR_ARG, "the float32 forward has no warp-per-pixel kernel");
     if (!L.bps) L.bps = opt.queue_dev ? 8 : kBpsOnePixelPerThread;
     e = launch_fwd_f32(P, detect_layout(*model), opt.kernel, opt.band_tails != 0, u, n_pix, OA, out_comps, out_total,
                        st, L);

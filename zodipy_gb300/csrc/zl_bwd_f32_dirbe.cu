@@ -11,12 +11,21 @@ cudaError_t launch_bwd_dirbe_cp(const KParamsF32& P, const KGradAux& A, const do
                                 const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
                                 int64_t n_tiles, cudaStream_t st, int64_t grid);
 
+// three or four spectral sets: zl_bwd_f32_dirbe34.cu (compiled in parallel with this file)
+cudaError_t launch_bwd_f32_dirbe34(const KParamsF32& P, const KGradAux& A, const double* u, int64_t n,
+                                   const ObsArgs& obs, const double* g_comps, const double* g_total, double* partials,
+                                   int64_t n_tiles, cudaStream_t st, int64_t grid);
+
 cudaError_t launch_bwd_f32_dirbe(const KParamsF32& P, const KGradAux& A, uint32_t flags, bool unpaired, const double* u,
                                  int64_t n, const ObsArgs& obs, const double* g_comps, const double* g_total,
                                  double* partials, int64_t n_tiles, cudaStream_t st, int64_t grid) {
   if (!unpaired && (flags & kBwdFlagsMask) == (kFlagsKelsall & kBwdFlagsMask))
     return launch_bwd_dirbe_cp(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
-  return launch_bwd_nspec<kLayoutDirbe, kFlagsRuntime>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+  switch (P.n_spec) {
+    case 1: return launch_groups<kLayoutDirbe, 1, kFlagsRuntime>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+    case 2: return launch_groups<kLayoutDirbe, 2, kFlagsRuntime>(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+    default: return launch_bwd_f32_dirbe34(P, A, u, n, obs, g_comps, g_total, partials, n_tiles, st, grid);
+  }
 }
 
 }  // namespace zl

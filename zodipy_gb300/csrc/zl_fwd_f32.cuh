@@ -186,7 +186,9 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
 
 }
 
-template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
+// MODE: the schedule the kernel is compiled for (kSchedStatic or kSchedQueue); one build
+// serving both ran the two-pixel kernel 7 % slower on the static schedule.
+template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS, int MODE>
 __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                       const double* __restrict__ u, int64_t n_pix,
                                                       const ObsArgs OA,
@@ -203,7 +205,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
   const int nc = L::generic ? P.n_comps : NC;
   const int nr = P.n_ranges;
 
-  ZL_SCHED_LOOP(kSchedAny, SC, n_pix, i) {
+  ZL_SCHED_LOOP(MODE, SC, n_pix, i) {
     // ---- per-pixel set-up -------------------------------------------------
     PixSetupF32<NC> PS;
     pixel_setup<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, OA, i, PS);
@@ -370,15 +372,19 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
       if (out_total) out_total[(int64_t)s * n_pix + col] = tot;
     }
   }
-  sched_finish<kSchedAny>(SC);
+  sched_finish<MODE>(SC);
 }
 
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS>
 static cudaError_t launch_f32_t(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs,
                                 double* oc, double* ot, cudaStream_t st, const LaunchArgs& L) {
   const size_t smem = sizeof(float4) * P.n_temps * NSPEC;
-  fwd_f32_kernel<NSPEC, LAYOUT, PRECISE, FLAGS>
-      <<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
+  if (L.sched.queue)
+    fwd_f32_kernel<NSPEC, LAYOUT, PRECISE, FLAGS, kSchedQueue>
+        <<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
+  else
+    fwd_f32_kernel<NSPEC, LAYOUT, PRECISE, FLAGS, kSchedStatic>
+        <<<(unsigned)fwd_grid(L, n), L.tpb, smem, st>>>(P, u, n, obs, oc, ot, L.sched);
   return cudaGetLastError();
 }
 
