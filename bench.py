@@ -80,9 +80,11 @@ def parse():
     p.add_argument("--large-nside", type=int, default=2048)
     p.add_argument(
         "--profile-case",
-        choices=["fwd", "bwd", "fwd-planck", "fwd64"],
+        choices=["fwd", "bwd", "fwd-planck", "fwd64", "fwd64-warp", "fwd-rrm", "bwd-rrm"],
         help="only run a few launches of one kernel of the workload (a target for ncu captures); no JSON",
     )
+    p.add_argument("--profile-degree", type=int, default=50,
+                   help="Gauss-Legendre degree of --profile-case (1 isolates the per-pixel work)")
     return p.parse_args()
 
 
@@ -368,23 +370,37 @@ def profile_case(args):
     from zodipy_gb300 import engine, packing
 
     u_np, obs, earth = workload(args.nside)
-    if args.profile_case == "fwd-planck":
+    if args.profile_case in ("fwd-planck", "fwd-rrm", "bwd-rrm"):
         import zodipy_gb300 as zg
         from zodipy_gb300 import units as un
 
-        model = zg.Model(857 * un.GHz, name="planck18", precision="float32")
+        if args.profile_case == "fwd-planck":
+            model = zg.Model(857 * un.GHz, name="planck18", precision="float32",
+                             gauss_quad_degree=args.profile_degree)
+        else:
+            model = zg.Model(25 * un.micron, name="rrm-experimental", precision="float32",
+                             gauss_quad_degree=args.profile_degree)
     else:
-        model = build_model("float64" if args.profile_case == "fwd64" else "float32")
+        import zodipy_gb300 as zg
+        from zodipy_gb300 import units as un
+
+        model = zg.Model(25 * un.micron, name="dirbe", gauss_quad_degree=args.profile_degree,
+                         precision="float64" if args.profile_case.startswith("fwd64") else "float32")
     zl = model.zl_model
     u = torch.from_numpy(u_np).cuda()
     tab = packing.observer_table(zl, obs, earth, [0], any_mode=False)
     obs_dev = engine.upload_observers(tab)
     g = torch.ones((1, u.shape[1]), dtype=torch.float64, device="cuda")
+    from zodipy_gb300 import _lib
+
+    warp = engine.launch_options(kernel=_lib.ZL_KERNEL_WARP_PER_PIXEL)
     for _ in range(max(args.steps, 1)):
-        if args.profile_case == "bwd":
+        if args.profile_case in ("bwd", "bwd-rrm"):
             engine.backward(zl, u, obs_dev, 1, g_total=g)
         elif args.profile_case == "fwd64":
             engine.forward(zl, u, obs_dev, 1, "float64")
+        elif args.profile_case == "fwd64-warp":
+            engine.forward(zl, u, obs_dev, 1, "float64", launch=warp)
         else:
             engine.forward(zl, u, obs_dev, 1, "float32")
     torch.cuda.synchronize()

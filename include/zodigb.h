@@ -372,6 +372,11 @@ ZL_API int zl_diag_atan2(const float* y_dev, const float* x_dev, float* out_dev,
  * against the conversion instruction. */
 ZL_API int zl_diag_d2f(const double* d_dev, float* out_dev, int64_t n, void* stream);
 
+/* Diagnostics: the kernels' float-to-double conversion of their results without float64
+ * instructions: out[i] = (double)f[i] for n device floats.  For checking it against the
+ * conversion instruction. */
+ZL_API int zl_diag_f2d(const float* f_dev, double* out_dev, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

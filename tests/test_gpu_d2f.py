@@ -73,3 +73,33 @@ def test_split_and_rounding_match_the_conversion(lib):
     np.testing.assert_array_equal(hi, want)
     # the pair keeps 47 significand bits (the last one sticky): |hi + lo - d| < 2^-45 |d|
     assert np.all(np.abs((hi + lo) - d) < 2.0**-45 * np.abs(d))
+
+
+def _float_cases():
+    """Float bit patterns: random ones over the whole range (normal, subnormal, inf, NaN of
+    either sign), every exponent, and the edges."""
+    rng = np.random.default_rng(7)
+    bits = rng.integers(0, 1 << 32, 1 << 20, dtype=np.uint64).astype(np.uint32)
+    expo = (np.arange(256, dtype=np.uint32) << 23) | rng.integers(0, 1 << 23, 256, dtype=np.uint64).astype(np.uint32)
+    edge = np.array([0x00000000, 0x80000000, 0x00000001, 0x807FFFFF, 0x00800000, 0x7F7FFFFF, 0xFF7FFFFF,
+                     0x7F800000, 0xFF800000, 0x7FC00000, 0x7F800001, 0x3F800000, 0xBF800000], dtype=np.uint32)
+    return np.concatenate([bits, expo, expo | 0x80000000, edge]).view(np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not cuda_ok(), reason="needs CUDA")
+def test_float_to_double_bits_match_the_conversion(lib):
+    """The kernels store their float results as doubles by bit operations (f2d_bits): the same
+    double as the conversion instruction for every float, NaN payloads included (they take
+    the instruction)."""
+    import torch
+
+    f = _float_cases()
+    fd = torch.from_numpy(f).cuda()
+    out = torch.empty(f.size, dtype=torch.float64, device="cuda")
+    rc = lib.zl_diag_f2d(ctypes.c_void_p(fd.data_ptr()), ctypes.c_void_p(out.data_ptr()), f.size,
+                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    got = out.cpu().numpy()
+    want = fd.double().cpu().numpy()  # the conversion instruction
+    np.testing.assert_array_equal(got.view(np.uint64), want.view(np.uint64))

@@ -202,6 +202,20 @@ __device__ __forceinline__ float d2f_bits(double d) {
   return ff_split(d).hi;  // the rounded value: ff_split renormalises its pair
 }
 
+// (double)f by bit operations, without a float64 instruction (GB300's FP64 pipe takes a
+// warp's conversion over tens of cycles, and every pixel converts each of its results): the
+// sign, the exponent re-biased from 127 to 1023 and the significand shifted into place; every
+// float is a double, so the value is the same.  Zero keeps its sign; subnormal floats, inf and
+// NaN take the conversion instruction.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int e = (b >> 23) & 0xffu;
+  if ((b & 0x7fffffffu) != 0u && e - 1u >= 254u) return (double)f;
+  const unsigned int hi = (b & 0x7fffffffu) ? (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((b & 0x7fffffu) >> 3)
+                                            : (b & 0x80000000u);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+
 // ff_mul without the final renormalisation: (p, e) with |e| <= ulp(p); the fast sums below
 // accept it as an operand
 __device__ __forceinline__ ff ff_mul_nr(ff a, ff b) {

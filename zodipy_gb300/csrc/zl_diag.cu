@@ -79,7 +79,20 @@ __global__ void d2f_eval(const double* __restrict__ d, float* __restrict__ out, 
   }
 }
 
+__global__ void f2d_eval(const float* __restrict__ f, double* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = zl::f2d_bits(f[i]);
+}
+
 }  // namespace
+
+extern "C" ZL_API int zl_diag_f2d(const float* f_dev, double* out_dev, int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && (!f_dev || !out_dev))) return ZL_ERR_ARG;
+  if (n == 0) return ZL_OK;
+  const int64_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  f2d_eval<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(f_dev, out_dev, n);
+  return cudaGetLastError() == cudaSuccess ? ZL_OK : ZL_ERR_CUDA;
+}
 
 extern "C" ZL_API int zl_diag_d2f(const double* d_dev, float* out_dev, int64_t n, void* stream) {
   if (n < 0 || (n > 0 && (!d_dev || !out_dev))) return ZL_ERR_ARG;

@@ -267,7 +267,9 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
       double tot = 0.0;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const double v = (double)(sums[c] * hsc[c]);
+        // the bit conversion measured 1.5 % faster without scattering and 5 % slower with
+        // it (the compiler schedules the two instantiations differently); same value either way
+        const double v = Fl::scat(P) ? (double)(sums[c] * hsc[c]) : f2d_bits(sums[c] * hsc[c]);
         if (out_comps) out_comps[((int64_t)s * NC + c) * n_pix + col] = v;
         tot = (c == 0) ? v : __dadd_rn(tot, v);
       }
