@@ -53,7 +53,10 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
   static_assert(((FLAGS >> (8 + CR)) & 3u) == 0u, "ring and feature centred on the Sun");
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
-  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);
+  __shared__ BwdObs<NC> s_obs;  // the observer set-up the block's pixels share
+  const int cached = bwd_obs_cache_index(OA, (int64_t)blockIdx.x * kTile, n_pix);
+  if (threadIdx.x == 0 && cached >= 0) bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, record_observer(OA, cached), s_obs);
+  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);  // its barrier also publishes s_obs
   const int nT = P.n_temps;
   const KCompF32& Cf = P.comp[CF];
 
@@ -65,7 +68,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
 
     if (i < n_pix) {
       BwdPix<NC, NSPEC> B;
-      bwd_pixel_setup<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, B);
+      bwd_pixel_setup_cached<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, cached, s_obs, B);
       const ff2 hsP = pack_ff(B.hs_r[RR], B.hs_r[RF]), mdP = pack_ff(B.mid_r[RR], B.mid_r[RF]);
       const ff2 waP = pack_ff(B.wa_c[CR], B.wa_c[CF]), wbP = pack_ff(B.wb_c[CR], B.wb_c[CF]);
       const float2 rrP = make_float2(B.rr_c[CR], B.rr_c[CF]);
@@ -280,7 +283,10 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
                 "bands 1 and 2 centred on the Sun, with p = 4 and their own inner-cutoff terms");
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
-  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);
+  __shared__ BwdObs<NC> s_obs;  // the observer set-up the block's pixels share
+  const int cached = bwd_obs_cache_index(OA, (int64_t)blockIdx.x * kTile, n_pix);
+  if (threadIdx.x == 0 && cached >= 0) bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, record_observer(OA, cached), s_obs);
+  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);  // its barrier also publishes s_obs
   const int nT = P.n_temps;
   const KCompF32& K1 = P.comp[C1];
   const KCompF32& K2 = P.comp[C2];
@@ -293,7 +299,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
 
     if (i < n_pix) {
       BwdPix<NC, NSPEC> B;
-      bwd_pixel_setup<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, B);
+      bwd_pixel_setup_cached<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, cached, s_obs, B);
       const float2 unP = make_float2(B.un_c[C1], B.un_c[C2]), onP = make_float2(B.on_c[C1], B.on_c[C2]);
       // q: delta_zeta [deg], v, p, delta_r, 1/delta_zeta [deg], -20/delta_r
       const float2 c1P = make_float2(K1.c[1], K2.c[1]), c2P = make_float2(K1.c[2], K2.c[2]);

@@ -206,6 +206,205 @@ __device__ __forceinline__ void bwd_pixel_setup(const KParamsF32& P, const doubl
   }
 }
 
+// What the adjoint's pixel set-up derives from the observer (and Earth) alone, for the
+// components in MASK: shared by the pixels of a block that have the same observer
+// (bwd_obs_setup once per block, bwd_pixel_setup_obs per pixel).  The operations are those of
+// bwd_pixel_setup, so the bits are the same either way.
+template <int NC>
+struct BwdObs {
+  ff ox, oy, oz, r2;
+  ff c_in[ZL_MAX_RANGES], c_out[ZL_MAX_RANGES];  // |X_obs|^2 - cutoff^2
+  ff dx[NC], dy[NC], dz[NC], d2[NC];             // X_obs - X_0 and its square
+  float on_c[NC];                                // (X_obs - X_0) . n
+  float cph[NC], sph[NC], rox[NC], roy[NC], eqx[NC], eqy[NC];  // the feature's frame
+  uint32_t outside;
+};
+
+template <uint32_t LAYOUT, uint32_t MASK, uint32_t FLAGS>
+__device__ __forceinline__ void bwd_obs_setup(const KParamsF32& P, const PixObs& O,
+                                              BwdObs<Lay<LAYOUT>::ncomp()>& Q) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<FLAGS>;
+  constexpr int NC = L::ncomp();
+  const int nr = P.n_ranges;
+  const ff ox = ff_split(O.ox), oy = ff_split(O.oy), oz = ff_split(O.oz);
+  Q.ox = ox;
+  Q.oy = oy;
+  Q.oz = oz;
+  Q.outside = O.outside;
+  const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+  Q.r2 = r2;
+#pragma unroll
+  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+    bool used = false;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
+    if (used && r < nr) {
+      Q.c_in[r] = ff_add(r2, ff_neg(ff{P.cut_in_hi[r], P.cut_in_lo[r]}));
+      Q.c_out[r] = ff_add(r2, ff_neg(ff{P.cut_out_hi[r], P.cut_out_lo[r]}));
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    Q.on_c[c] = Q.cph[c] = Q.sph[c] = Q.rox[c] = Q.roy[c] = Q.eqx[c] = Q.eqy[c] = 0.f;
+    if (!((MASK >> c) & 1u)) continue;
+    const KCompF32& C = P.comp[c];
+    const int type = L::type(c);
+    const bool off = Fl::offset(C, c);
+    const ff dx = ff_add_fast(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add_fast(oy, ff{-C.oy, -C.oy_lo}),
+             dz = ff_add_fast(oz, ff{-C.oz, -C.oz_lo});
+    Q.dx[c] = dx;
+    Q.dy[c] = dy;
+    Q.dz[c] = dz;
+    if (c > 0 && ((MASK >> (c - 1)) & 1u) && C.same_plane_prev) {
+      Q.on_c[c] = Q.on_c[c - 1];
+    } else {
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      const ff on = ff_add_fast(ff_add_fast(ff_mul_nr(dx, nx), ff_mul_nr(dy, ny)), ff_mul_nr(dz, nz));
+      Q.on_c[c] = on.hi + on.lo;
+    }
+    Q.d2[c] = !off ? r2 : ff_add_fast(ff_add_fast(ff_mul_nr(dx, dx), ff_mul_nr(dy, dy)), ff_mul_nr(dz, dz));
+    if (type == ZL_FEATURE) {
+      const ff exf = ff_add_fast(ff_split(O.ex), ff{-C.ox, -C.ox_lo}), eyf = ff_add_fast(ff_split(O.ey), ff{-C.oy, -C.oy_lo});
+      const float ex = exf.hi + exf.lo, ey = eyf.hi + eyf.lo;
+      const float phi = atan2f(ey, ex) + C.c[6];
+      float sp, cp;
+      sincosf(phi, &sp, &cp);
+      const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+      Q.cph[c] = cp;
+      Q.sph[c] = sp;
+      Q.rox[c] = cp * ocx + sp * ocy;
+      Q.roy[c] = cp * ocy - sp * ocx;
+      const float e2 = ex * ex + ey * ey;
+      Q.eqx[c] = ey / e2;
+      Q.eqy[c] = -ex / e2;
+    }
+  }
+}
+
+// Pixel i's adjoint set-up from its observer's (Q): bwd_pixel_setup's operations.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
+__device__ __forceinline__ void bwd_pixel_setup_obs(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
+                                                    const double* __restrict__ g_comps,
+                                                    const double* __restrict__ g_total, int64_t i,
+                                                    const BwdObs<Lay<LAYOUT>::ncomp()>& Q,
+                                                    BwdPix<Lay<LAYOUT>::ncomp(), NSPEC>& B) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<FLAGS>;
+  constexpr int NC = L::ncomp();
+  const int nr = P.n_ranges;
+  const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
+  const ff ox = Q.ox, oy = Q.oy, oz = Q.oz;
+  const uint32_t outside = Q.outside;
+  B.uxf = ux.hi, B.uyf = uy.hi, B.uzf = uz.hi;
+  B.oxf = ox.hi, B.oyf = oy.hi, B.ozf = oz.hi;
+  const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
+  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
+  B.beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));
+#pragma unroll
+  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+    bool used = false;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
+    if (used && r < nr) {
+      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_in[r]);
+      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_out[r]);
+      B.hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+      B.mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+    } else {
+      B.hs_r[r] = B.mid_r[r] = ff{0.f, 0.f};
+    }
+  }
+  B.bperp = 0.f;
+  if (SCAT) {
+    const float cx = B.uyf * B.ozf - B.uzf * B.oyf, cy = B.uzf * B.oxf - B.uxf * B.ozf,
+                cz = B.uxf * B.oyf - B.uyf * B.oxf;
+    B.bperp = sqrtf(cx * cx + cy * cy + cz * cz);
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    B.un_c[c] = B.on_c[c] = 0.f;
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s) B.gup[c][s] = 0.f;
+    B.wa_c[c] = B.wb_c[c] = ff{0.f, 0.f};
+    B.rr_c[c] = 0.f;
+    B.rux[c] = B.ruy[c] = B.rox[c] = B.roy[c] = B.eqx[c] = B.eqy[c] = 0.f;
+    if (!((MASK >> c) & 1u)) continue;
+    const KCompF32& C = P.comp[c];
+    const int type = L::type(c);
+    const ff hs = B.hs_r[L::range(c)], md = B.mid_r[L::range(c)];
+    const bool off = Fl::offset(C, c);
+    if (c > 0 && ((MASK >> (c - 1)) & 1u) && C.same_plane_prev) {  // the ring's plane, for the feature
+      B.un_c[c] = B.un_c[c - 1];
+    } else {
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      const ff un = ff_add_fast(ff_add_fast(ff_mul_nr(ux, nx), ff_mul_nr(uy, ny)), ff_mul_nr(uz, nz));
+      B.un_c[c] = un.hi + un.lo;
+    }
+    B.on_c[c] = Q.on_c[c];
+    const float hsf = hs.hi + hs.lo;
+#pragma unroll
+    for (int s = 0; s < NSPEC; ++s)
+      B.gup[c][s] =
+          d2f_bits(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) * hsf;
+    if (type == ZL_RING || type == ZL_FEATURE) {
+      const ff dx = Q.dx[c], dy = Q.dy[c], dz = Q.dz[c];
+      const ff beta =
+          !off ? B.beta_h : ff_add_fast(ff_add_fast(ff_mul_nr(dx, ux), ff_mul_nr(dy, uy)), ff_mul_nr(dz, uz));
+      const ff wm = ff_add_fast(md, beta);
+      const ff cw = ff_add_fast(ff_add_fast(Q.d2[c], ff_neg(ff_mul_nr(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
+      const ff w0 = cw.hi < 0.f ? ff_sqrt(ff_neg(cw)) : ff{0.f, 0.f};
+      B.wa_c[c] = ff_add_fast(wm, ff_neg(w0));
+      B.wb_c[c] = ff_add_fast(wm, w0);
+      const ff res = ff_add_fast(ff_mul_nr(w0, w0), cw);
+      B.rr_c[c] = res.hi + res.lo;
+    }
+    if (type == ZL_FEATURE) {
+      const float cp = Q.cph[c], sp = Q.sph[c];
+      B.rux[c] = cp * B.uxf + sp * B.uyf;
+      B.ruy[c] = cp * B.uyf - sp * B.uxf;
+      B.rox[c] = Q.rox[c];
+      B.roy[c] = Q.roy[c];
+      B.eqx[c] = Q.eqx[c];
+      B.eqy[c] = Q.eqy[c];
+    }
+  }
+}
+
+// The adjoint's observer set-up of pixel i, out of line (see observer_setup_own).
+template <uint32_t LAYOUT, uint32_t MASK, uint32_t FLAGS>
+__device__ __noinline__ void bwd_obs_setup_own(const KParamsF32& P, const ObsArgs& OA, int64_t i, int64_t n_pix,
+                                               BwdObs<Lay<LAYOUT>::ncomp()>* Q) {
+  bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, pixel_observer(OA, i, n_pix), *Q);
+}
+
+// Pixel i's adjoint set-up: from its block's shared observer set-up when it has the same
+// observer (obs_cache_hit), else from its own.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
+__device__ __forceinline__ void bwd_pixel_setup_cached(const KParamsF32& P, const double* __restrict__ u,
+                                                       int64_t n_pix, const ObsArgs& OA,
+                                                       const double* __restrict__ g_comps,
+                                                       const double* __restrict__ g_total, int64_t i, int cached,
+                                                       const BwdObs<Lay<LAYOUT>::ncomp()>& shared,
+                                                       BwdPix<Lay<LAYOUT>::ncomp(), NSPEC>& B) {
+  BwdObs<Lay<LAYOUT>::ncomp()> own;
+  const BwdObs<Lay<LAYOUT>::ncomp()>* q = &shared;
+  if (!(cached >= 0 && (OA.n_rec == 1 || find_observer(OA.rec, OA.n_rec, i) == cached))) {
+    bwd_obs_setup_own<LAYOUT, MASK, FLAGS>(P, OA, i, n_pix, &own);
+    q = &own;
+  }
+  bwd_pixel_setup_obs<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, g_comps, g_total, i, *q, B);
+}
+
+// The observer record a block of the adjoint shares (-1: none): a one-observer call's record,
+// or the record of the block's first tile's first pixel.  Block-uniform.
+__device__ __forceinline__ int bwd_obs_cache_index(const ObsArgs& OA, int64_t first_pixel, int64_t n_pix) {
+  if (!OA.rec) return -1;
+  if (OA.n_rec == 1) return 0;
+  if (first_pixel >= n_pix) return -1;
+  return find_observer(OA.rec, OA.n_rec, first_pixel);
+}
+
 // One LOS range at one quadrature node: position, distance from the Sun, grain
 // temperature, blackbody value and slope per spectral set, scattering terms.
 template <int NSPEC>
@@ -568,7 +767,10 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
   constexpr int NG = G::NG;
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
-  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);
+  __shared__ BwdObs<NC> s_obs;  // the observer set-up the block's pixels share
+  const int cached = bwd_obs_cache_index(OA, (int64_t)blockIdx.x * kTile, n_pix);
+  if (threadIdx.x == 0 && cached >= 0) bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, record_observer(OA, cached), s_obs);
+  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);  // its barrier also publishes s_obs
   const int nT = P.n_temps;
 
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
@@ -579,7 +781,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
 
     if (i < n_pix) {
       BwdPix<NC, NSPEC> B;
-      bwd_pixel_setup<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, B);
+      bwd_pixel_setup_cached<LAYOUT, MASK, NSPEC, SCAT, FLAGS>(P, u, n_pix, OA, g_comps, g_total, i, cached, s_obs, B);
       // Offset and orientation derivatives: with X - X_0 = R_los u + (X_obs - X_0) they are
       // combinations of four per-node sums per component, completed after the node loop.
       float fthx[NC], fthy[NC];

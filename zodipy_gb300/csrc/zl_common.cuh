@@ -325,6 +325,12 @@ struct PixObs {
   uint32_t outside;
 };
 
+// Observer record o as a pixel's observer.
+__device__ __forceinline__ PixObs record_observer(const ObsArgs& OA, int o) {
+  const ZlObserver& O = OA.rec[o];
+  return PixObs{O.obs[0], O.obs[1], O.obs[2], O.earth[0], O.earth[1], O.outside};
+}
+
 __device__ __forceinline__ PixObs pixel_observer(const ObsArgs& A, int64_t i, int64_t n_pix) {
   PixObs p;
   if (A.rec) {

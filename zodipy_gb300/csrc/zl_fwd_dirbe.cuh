@@ -80,8 +80,11 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
   constexpr int NC = 6;
   constexpr int MODE = QUEUE ? kSchedQueue : kSchedStatic;
   extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
+  __shared__ ObsSetupF32<NC> s_obs;   // the observer set-up the block's pixels share
   const int nT = P.n_temps;
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  const int cached = obs_cache_index<MODE>(OA, (int64_t)blockIdx.x * blockDim.x, n_pix);
+  if (threadIdx.x == 0 && cached >= 0) observer_setup<kLayoutDirbe, FLAGS, NC>(P, record_observer(OA, cached), s_obs);
   __syncthreads();
 
   const KCompF32& Cc = P.comp[0];
@@ -93,7 +96,7 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
 
   ZL_SCHED_LOOP(MODE, SC, n_pix, i) {
     PixSetupF32<NC> PS;
-    pixel_setup<kLayoutDirbe, FLAGS, true, NC>(P, u, n_pix, OA, i, PS);
+    pixel_setup_cached<kLayoutDirbe, FLAGS, true, NC>(P, u, n_pix, OA, i, cached, s_obs, PS);
     const ff2 z1b = pack_ff(PS.z1[1], PS.z1[2]), z0b = pack_ff(PS.z0[1], PS.z0[2]);
     const ff2 hsq = pack_ff(PS.hs[4], PS.hs[5]), mhq = pack_ff(PS.mh[4], PS.mh[5]);
     const ff2 z1q = pack_ff(PS.z1[4], PS.z1[5]), z0q = pack_ff(PS.z0[4], PS.z0[5]);

@@ -46,6 +46,195 @@ struct PixSetupF32 {
   float b2h, bperp;
 };
 
+// What a pixel's set-up derives from its observer (and Earth) alone: the same for every
+// pixel of one observer, so a block derives it once and shares it (see obs_cache_index).
+// The operations are those of the per-pixel set-up, so the bits are the same either way.
+template <int NC>
+struct ObsSetupF32 {
+  ff ox, oy, oz;                                 // observer position
+  ff r2;                                         // |X_obs|^2
+  ff c_in[ZL_MAX_RANGES], c_out[ZL_MAX_RANGES];  // |X_obs|^2 - cutoff^2 of each range's spheres
+  ff dx[NC], dy[NC], dz[NC];                     // X_obs - X_0
+  ff on[NC];                                     // (X_obs - X_0) . n
+  ff d2[NC];                                     // |X_obs - X_0|^2
+  float rox[NC], roy[NC], cph[NC], sph[NC];      // features: X_obs - X_0 in the frame rotated by phi
+  uint32_t outside;
+};
+
+template <uint32_t LAYOUT, uint32_t FLAGS, int NC>
+__device__ __forceinline__ void observer_setup(const KParamsF32& P, const PixObs& O, ObsSetupF32<NC>& Q) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
+  const int nc = L::generic ? P.n_comps : NC;
+  const int nr = P.n_ranges;
+  const ff ox = ff_split(O.ox), oy = ff_split(O.oy), oz = ff_split(O.oz);
+  Q.ox = ox;
+  Q.oy = oy;
+  Q.oz = oz;
+  Q.outside = O.outside;
+  const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
+  Q.r2 = r2;
+#pragma unroll
+  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+    if (r < nr) {
+      Q.c_in[r] = ff_add(r2, ff_neg(ff{P.cut_in_hi[r], P.cut_in_lo[r]}));
+      Q.c_out[r] = ff_add(r2, ff_neg(ff{P.cut_out_hi[r], P.cut_out_lo[r]}));
+    }
+  }
+  ff on = {0.f, 0.f};  // (X_obs - X_0) . n of the previous component
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    if (c >= nc) break;
+    const KCompF32& C = P.comp[c];
+    const int type = L::generic ? C.type : L::type(c);
+    const bool off = Fl::offset(C, c);
+    // X_obs - X_0 (exact for the components centred on the Sun)
+    const ff dx = ff_add_fast(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add_fast(oy, ff{-C.oy, -C.oy_lo}),
+             dz = ff_add_fast(oz, ff{-C.oz, -C.oz_lo});
+    Q.dx[c] = dx;
+    Q.dy[c] = dy;
+    Q.dz[c] = dz;
+    // kept from the previous component when it has the same plane and centre
+    if (!(c > 0 && C.same_plane_prev)) {
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      on = ff_add_fast(ff_add_fast(ff_mul_nr(dx, nx), ff_mul_nr(dy, ny)), ff_mul_nr(dz, nz));
+    }
+    Q.on[c] = on;
+    Q.d2[c] = !off ? r2 : ff_add_fast(ff_add_fast(ff_mul_nr(dx, dx), ff_mul_nr(dy, dy)), ff_mul_nr(dz, dz));
+    Q.rox[c] = Q.roy[c] = Q.cph[c] = Q.sph[c] = 0.f;
+    if (featurelike(type)) {
+      // longitude relative to Earth's, minus theta (number_density.py:167-173): rotate the
+      // frame by phi = atan2(earth - X_0) + theta so the wrapped difference is one atan2 of
+      // two coordinates that are linear in the node abscissa
+      const ff ex = ff_add_fast(ff_split(O.ex), ff{-C.ox, -C.ox_lo}), ey = ff_add_fast(ff_split(O.ey), ff{-C.oy, -C.oy_lo});
+      const float phi = atan2f(ey.hi + ey.lo, ex.hi + ex.lo) + C.c[6];
+      float sp, cp;
+      sincosf(phi, &sp, &cp);
+      const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
+      Q.cph[c] = cp;
+      Q.sph[c] = sp;
+      Q.rox[c] = cp * ocx + sp * ocy;
+      Q.roy[c] = cp * ocy - sp * ocx;
+    }
+  }
+}
+
+// Pixel i's set-up from its observer's (Q).
+template <uint32_t LAYOUT, uint32_t FLAGS, bool PRECISE, int NC>
+__device__ __forceinline__ void pixel_setup_obs(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
+                                                int64_t i, const ObsSetupF32<NC>& Q, PixSetupF32<NC>& S) {
+  using L = Lay<LAYOUT>;
+  using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
+  const int nc = L::generic ? P.n_comps : NC;
+  const int nr = P.n_ranges;
+  // float-float values of the doubles by bit operations (no float64 instruction); the sums
+  // below are ff_add_fast (accurate to a few 2^-48 of their operands: the geometry needs
+  // absolute, not relative, accuracy), except where the cutoff spheres are intersected
+  const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
+  const ff ox = Q.ox, oy = Q.oy, oz = Q.oz;
+  const uint32_t outside = Q.outside;
+  const float uxf = ux.hi, uyf = uy.hi;
+
+  const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
+  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
+  const ff r2 = Q.r2;
+  const ff beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));  // u . X_obs
+
+  ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];
+#pragma unroll
+  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
+    if (r < nr) {
+      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_in[r]);
+      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_out[r]);
+      hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
+      mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+    } else {
+      hs_r[r] = ff{0.f, 0.f};
+      mid_r[r] = ff{0.f, 0.f};
+    }
+  }
+
+  // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
+  const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
+  const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
+  // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
+  S.b2h = b2h;
+  S.bperp = Fl::scat(P) ? sqrtf(b2h) : 0.f;
+
+  // per-component set-up
+  ff un = {0.f, 0.f};  // u . n of the previous component
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    if (c >= nc) break;
+    const KCompF32& C = P.comp[c];
+    const int type = L::generic ? C.type : L::type(c);
+    ff hs = {0.f, 0.f}, md = {0.f, 0.f};
+    if (!L::generic) {
+      hs = hs_r[L::range(c)];
+      md = mid_r[L::range(c)];
+    } else {
+#pragma unroll
+      for (int r = 0; r < ZL_MAX_RANGES; ++r)
+        if (r == C.range) {
+          hs = hs_r[r];
+          md = mid_r[r];
+        }
+    }
+    S.hs[c] = hs;
+    S.mh[c] = ff_add_fast(md, beta_h);  // R_los + u . X_obs = hs x + mh
+    const bool off = Fl::offset(C, c);
+    // height above the symmetry plane, linear in the node abscissa x:
+    //   Z = (hs x + mid)(u . n) + (X_obs - X_0) . n = z1 x + z0
+    // (u . n is kept from the previous component when it has the same plane, as the ring and
+    // the Earth-trailing feature do)
+    if (!(c > 0 && C.same_plane_prev)) {
+      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
+      un = ff_add_fast(ff_add_fast(ff_mul_nr(ux, nx), ff_mul_nr(uy, ny)), ff_mul_nr(uz, nz));
+    }
+    S.z1[c] = ff_mul(hs, un);
+    S.z0[c] = ff_add_fast(ff_mul_nr(md, un), Q.on[c]);
+    // |X - X_0|^2 = w^2 + b^2,  w = hs x + (mid + beta),  beta = u . (X_obs - X_0),
+    // b^2 = |X_obs - X_0|^2 - beta^2;  the ring/feature use w^2 + c' with c' = b^2 - R0^2
+    S.wm[c] = S.mh[c];
+    S.b2[c] = b2h;
+    S.cw[c] = ff{0.f, 0.f};
+    S.wa[c] = S.wb[c] = ff{0.f, 0.f};
+    S.rr[c] = 0.f;
+    if (off || (PRECISE && ringlike(type)) || masked(type)) {
+      const ff dx = Q.dx[c], dy = Q.dy[c], dz = Q.dz[c];
+      const ff beta =
+          !off ? beta_h : ff_add_fast(ff_add_fast(ff_mul_nr(dx, ux), ff_mul_nr(dy, uy)), ff_mul_nr(dz, uz));
+      const ff bb = ff_add_fast(Q.d2[c], ff_neg(ff_mul_nr(beta, beta)));
+      S.wm[c] = ff_add_fast(md, beta);
+      S.b2[c] = fmaxf(bb.hi + bb.lo, 0.f);
+      S.cw[c] = masked(type) ? bb : ff_add_fast(bb, ff_neg(ff{C.c[4], C.c[5]}));
+      if (ringlike(type)) {
+        // R^2 - R0^2 = w^2 + c' = (w - w0)(w + w0) + (w0^2 + c'),  w0 = sqrt(max(-c', 0)):
+        // each factor is linear in the node abscissa and evaluated to ~1 ulp near its zero
+        const ff w0 = S.cw[c].hi < 0.f ? ff_sqrt(ff_neg(S.cw[c])) : ff{0.f, 0.f};
+        S.wa[c] = ff_add_fast(S.wm[c], ff_neg(w0));
+        S.wb[c] = ff_add_fast(S.wm[c], w0);
+        const ff res = ff_add_fast(ff_mul_nr(w0, w0), S.cw[c]);
+        S.rr[c] = res.hi + res.lo;
+      }
+    }
+    S.fx1[c] = S.fx0[c] = S.fy1[c] = S.fy0[c] = 0.f;
+    if (featurelike(type)) {
+      const float cp = Q.cph[c], sp = Q.sph[c];
+      const float rux = cp * uxf + sp * uyf, ruy = cp * uyf - sp * uxf;
+      const float h = hs.hi + hs.lo, m = md.hi + md.lo;
+      S.fx1[c] = h * rux;
+      S.fx0[c] = fmaf(m, rux, Q.rox[c]);
+      S.fy1[c] = h * ruy;
+      S.fy0[c] = fmaf(m, ruy, Q.roy[c]);
+    }
+  }
+}
+
+// Pixel i's set-up with its observer's part evaluated in place (the same operations as
+// observer_setup + pixel_setup_obs, interleaved so that each observer quantity is consumed
+// where it is formed: splitting them kept the generic layout's eighty-odd observer values
+// alive at once and spilled).
 template <uint32_t LAYOUT, uint32_t FLAGS, bool PRECISE, int NC>
 __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
                                             const ObsArgs& OA, int64_t i, PixSetupF32<NC>& S) {
@@ -186,6 +375,48 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
 
 }
 
+// The observer record whose set-up a block derives once and shares (-1: none, every pixel
+// derives its own): the only record of a one-observer call, else the record of the block's first
+// pixel on the static schedule (a batch's observers own long runs of pixels); none with the
+// work queue, whose tiles come in any order, or for time-ordered calls.  Block-uniform.
+template <int MODE>
+__device__ __forceinline__ int obs_cache_index(const ObsArgs& OA, int64_t first_pixel, int64_t n_pix) {
+  if (!OA.rec) return -1;
+  if (OA.n_rec == 1) return 0;
+  if (MODE != kSchedStatic || first_pixel >= n_pix) return -1;
+  return find_observer(OA.rec, OA.n_rec, first_pixel);
+}
+
+// Whether pixel i takes its block's shared observer set-up.
+__device__ __forceinline__ bool obs_cache_hit(const ObsArgs& OA, int cached, int64_t i) {
+  return cached >= 0 && (OA.n_rec == 1 || find_observer(OA.rec, OA.n_rec, i) == cached);
+}
+
+// Pixel i's own observer set-up, out of line: a second inlined copy of the set-up next to the
+// shared one raised the DIRBE forward kernel from 95 to 121 registers (four instead of five
+// blocks per SM).  Q is the caller's local memory; only the pixels that do not share their
+// block's observer (and time-ordered calls) come here.
+template <uint32_t LAYOUT, uint32_t FLAGS, int NC>
+__device__ __noinline__ void observer_setup_own(const KParamsF32& P, const ObsArgs& OA, int64_t i, int64_t n_pix,
+                                                ObsSetupF32<NC>* Q) {
+  observer_setup<LAYOUT, FLAGS, NC>(P, pixel_observer(OA, i, n_pix), *Q);
+}
+
+// Pixel i's set-up: from its block's shared observer set-up when it has the same observer,
+// else from its own.
+template <uint32_t LAYOUT, uint32_t FLAGS, bool PRECISE, int NC>
+__device__ __forceinline__ void pixel_setup_cached(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
+                                                   const ObsArgs& OA, int64_t i, int cached,
+                                                   const ObsSetupF32<NC>& shared, PixSetupF32<NC>& S) {
+  ObsSetupF32<NC> own;
+  const ObsSetupF32<NC>* q = &shared;
+  if (!obs_cache_hit(OA, cached, i)) {
+    observer_setup_own<LAYOUT, FLAGS, NC>(P, OA, i, n_pix, &own);
+    q = &own;
+  }
+  pixel_setup_obs<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, i, *q, S);
+}
+
 // MODE: the schedule the kernel is compiled for (kSchedStatic or kSchedQueue); one build
 // serving both ran the two-pixel kernel 7 % slower on the static schedule.
 template <int NSPEC, uint32_t LAYOUT, bool PRECISE, uint32_t FLAGS, int MODE>
@@ -198,8 +429,15 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
   using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
   constexpr int NC = L::ncomp();
   extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
+  // the observer set-up the block's pixels share; not for the generic layout (the RRM model),
+  // which measured 1.6 % slower with it (its eight components' set-up in shared memory)
+  constexpr bool kShared = !L::generic;
+  __shared__ ObsSetupF32<NC> s_obs;
   const int nT = P.n_temps;
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
+  const int cached = kShared ? obs_cache_index<MODE>(OA, (int64_t)blockIdx.x * blockDim.x, n_pix) : -1;
+  if (kShared && threadIdx.x == 0 && cached >= 0)
+    observer_setup<LAYOUT, FLAGS, NC>(P, record_observer(OA, cached), s_obs);
   __syncthreads();
 
   const int nc = L::generic ? P.n_comps : NC;
@@ -208,7 +446,10 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
   ZL_SCHED_LOOP(MODE, SC, n_pix, i) {
     // ---- per-pixel set-up -------------------------------------------------
     PixSetupF32<NC> PS;
-    pixel_setup<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, OA, i, PS);
+    if (kShared)
+      pixel_setup_cached<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, OA, i, cached, s_obs, PS);
+    else
+      pixel_setup<LAYOUT, FLAGS, PRECISE, NC>(P, u, n_pix, OA, i, PS);
     const ff* hs_c = PS.hs;
     const ff* mh_c = PS.mh;
     const ff* z1_c = PS.z1;

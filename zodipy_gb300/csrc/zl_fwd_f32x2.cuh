@@ -53,7 +53,7 @@ __host__ __device__ constexpr bool bands_centred() {
 // both (kSchedAny) ran 7 % slower on the static schedule (batched random directions, 15.61 ms
 // against 14.54 ms).
 template <int NSPEC, uint32_t LAYOUT, uint32_t FLAGS, bool TAILS, int MODE>
-__global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ KParamsF32 P,
+__global__ void __launch_bounds__(128, (NSPEC == 1 && LAYOUT == kLayoutPlanck) ? 4 : 0) fwd_f32x2_kernel(const __grid_constant__ KParamsF32 P,
                                                         const double* __restrict__ u, int64_t n_pix,
                                                         int64_t n_items, const ObsArgs OA,
                                                         double* __restrict__ out_comps,
@@ -65,9 +65,6 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
   extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
   const int nT = P.n_temps;
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
-  __syncthreads();
-
-  static_assert(!TAILS || bands_centred<LAYOUT, FLAGS>(), "band tails assume bands centred on the Sun");
   // Halves (static schedule without band tails): item j evaluates pixels j and j + n_items,
   // n_items = ceil(n_pix / 2).  Tiles (otherwise): n_items = TL x the number of 2 TL-pixel
   // tiles (TL: the schedule's tile), item j of tile k evaluates pixels 2 TL k + j and
@@ -76,6 +73,21 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
   // 1.6 % faster on the batched random-direction workload.
   constexpr bool kHalves = MODE == kSchedStatic && !TAILS;
   const int64_t TL = sched_tile(SC);
+  // the observer set-ups the block's first lanes .x and .y share (the two halves of a batch
+  // usually belong to different observers): warps 0 and 1 derive one each.  The Planck layout
+  // only: the DIRBE layout's two-pixel kernel (not its default) spilled with them at 168
+  // registers and keeps the per-pixel set-up.
+  constexpr bool kShared = LAYOUT == kLayoutPlanck;
+  __shared__ ObsSetupF32<NC> s_obs[kShared ? 2 : 1];
+  const int64_t first_a = kHalves ? (int64_t)blockIdx.x * blockDim.x : 2 * (int64_t)blockIdx.x * blockDim.x;
+  const int64_t first_b = kHalves ? first_a + n_items : first_a + TL;
+  const int cached_a = kShared ? obs_cache_index<MODE>(OA, first_a, n_pix) : -1;
+  const int cached_b = kShared ? obs_cache_index<MODE>(OA, first_b, n_pix) : -1;
+  if (kShared && threadIdx.x == 0 && cached_a >= 0)
+    observer_setup<LAYOUT, FLAGS, NC>(P, record_observer(OA, cached_a), s_obs[0]);
+  if (kShared && threadIdx.x == (blockDim.x > 32 ? 32u : 0u) && cached_b >= 0)
+    observer_setup<LAYOUT, FLAGS, NC>(P, record_observer(OA, cached_b), s_obs[kShared ? 1 : 0]);
+  __syncthreads();
   ZL_SCHED_LOOP(MODE, SC, n_items, item) {
     const int64_t ia = kHalves ? item : item + ZL_SCHED_TILE_BASE(MODE, SC, item);
     if (ia >= n_pix) continue;
@@ -87,8 +99,13 @@ __global__ void __launch_bounds__(128) fwd_f32x2_kernel(const __grid_constant__ 
     float2 b2h, bperp;
     {
       PixSetupF32<NC> A, B;
-      pixel_setup<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ia, A);
-      pixel_setup<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ib, B);
+      if (kShared) {
+        pixel_setup_cached<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ia, cached_a, s_obs[0], A);
+        pixel_setup_cached<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ib, cached_b, s_obs[kShared ? 1 : 0], B);
+      } else {
+        pixel_setup<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ia, A);
+        pixel_setup<LAYOUT, FLAGS, true, NC>(P, u, n_pix, OA, ib, B);
+      }
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         hs[c] = pack_ff(A.hs[c], B.hs[c]);
