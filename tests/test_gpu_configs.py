@@ -11,6 +11,8 @@ the maximum and median errors printed (run pytest with -s to see them):
   2  DIRBE over 64 wavelengths 80-130 um (Gaussian weights), nside 512 (3,145,728 LOS),
      observer (0.7071, 0.7071, 0) AU: float32 vs float64 kernel on every pixel, and the
      float64 kernel vs the oracle on 100,000 seeded pixels
+  -  the headline: DIRBE 25 um, nside 512, observer (0.7071, 0.7071, 0) AU: float32 vs
+     float64 on every pixel, float64 vs the oracle on 100,000 seeded pixels
   3  planck18 857 GHz, 256 observers with 10,000-500,000 random directions each (68.9 M
      LOS) in one batched launch: float32 vs float64 kernel on every LOS, float64 vs the
      oracle on 8 observers x 64 directions
@@ -138,6 +140,35 @@ def test_config2_bandpass_nside512_float32_vs_float64_and_oracle(lib):
     del c32, c64
     ref = oracle(desc, u[:, idx_t].cpu().numpy(), OBS2)
     assert_f64_close(sub, ref, "config 2 (100,000 of 3,145,728 LOS)")
+
+
+def test_headline_dirbe25_nside512_float32_vs_float64_and_oracle(lib):
+    """The workload the throughput is quoted on: DIRBE 25 um, nside 512, observer (0.7071,
+    0.7071, 0) AU, GL 50.  The default float32 kernel (component pairs, band tails, the block's
+    shared observer set-up) against the float64 kernel on every pixel, and the float64 kernel
+    against the oracle on 100,000 seeded pixels."""
+    import torch
+
+    from zodipy_gb300 import engine, packing
+    from zodipy_gb300.healpix import pix2vec_ring_torch
+
+    model = _model(25.0)
+    desc = same_inputs(model, workloads.oracle_desc("dirbe", "dirbe_25um", 50))
+    u = pix2vec_ring_torch(512, "cuda")
+    n = u.shape[1]
+    zl = model.zl_model
+    obs = engine.upload_observers(packing.observer_table(zl, OBS2, EARTH, [0], any_mode=False))
+    c64, _ = engine.forward(zl, u, obs, 1, "float64", want_total=False)
+    c32, _ = engine.forward(zl, u, obs, 1, "float32", want_total=False)
+    e_max, e_med, e_comp = f32_errors(c32[0], c64[0])
+    print(f"headline: float32 vs float64 total max {e_max:.3e} median {e_med:.3e}, component max {e_comp:.3e}")
+    assert e_max <= F32_RTOL and e_comp <= F32_RTOL
+    idx = np.sort(np.random.default_rng(5).choice(n, 100_000, replace=False))
+    idx_t = torch.from_numpy(idx).cuda()
+    sub = c64[0][:, idx_t].cpu().numpy()
+    del c32, c64
+    ref = oracle(desc, u[:, idx_t].cpu().numpy(), OBS2)
+    assert_f64_close(sub, ref, "headline (100,000 of 3,145,728 LOS)")
 
 
 def test_config3_batch_float32_vs_float64_every_los(lib):
