@@ -144,3 +144,29 @@ def test_device_tensors_stay_on_device(lib):
     assert out.is_cuda and out.dtype == torch.float64
     host = model.evaluate_xyz(case["unit_vectors"], case["obs"], case["earth"], return_comps=True)
     np.testing.assert_array_equal(out.cpu().numpy(), host)
+
+
+def test_host_calls_restage_the_observer_when_it_changes(lib):
+    """Host arrays go through the zero-copy path, which keeps the last observer record staged
+    per thread: alternating observers, a changed Earth, and alternating models whose cutoff
+    spheres (and so the record's cutoff flags) differ must each give the device path's bits."""
+    import torch
+
+    import zodipy_gb300 as zg
+    from zodipy_gb300 import units as un
+
+    case = load_case("dirbe25_nside8")
+    dirbe = product_model(case, "float32")
+    planck = zg.Model(857 * un.GHz, name="planck18", precision="float32")
+    u = case["unit_vectors"]
+    u_dev = torch.from_numpy(u).cuda()
+    cases = [(np.array([1.0, 0.0, 0.0]), np.array([1.0, 0.0, 0.0])),
+             (np.array([0.0, 1.6, 0.0]), np.array([0.0, 1.0, 0.0])),   # beyond the ring's and feature's spheres
+             (np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0])),   # the first observer, another Earth
+             (np.array([1.0, 0.0, 0.0]), np.array([1.0, 0.0, 0.0]))]
+    for _ in range(2):
+        for obs, earth in cases:
+            for model in (dirbe, dirbe, planck):  # a repeated call, then another model, same observer
+                host = model.evaluate_xyz(u, obs, earth, return_comps=True)
+                dev = model.evaluate_xyz(u_dev, obs, earth, return_comps=True).cpu().numpy()
+                np.testing.assert_array_equal(host, dev)

@@ -15,12 +15,13 @@ libzodigb's CUDA kernels:
 
 from __future__ import annotations
 
+import ctypes
 import threading
 
 import numpy as np
 from scipy import integrate
 
-from . import engine, packing
+from . import _lib, engine, packing
 from .components import ComponentLabel
 from .coords import SkyCoord as _LiteSkyCoord
 from .ephemeris import body_position
@@ -339,23 +340,25 @@ class Model:
             raise ValueError("positions must be (3,) or (3, ncoords)")
         per_pixel = obs.shape[1] > 1 or earth.shape[1] > 1
         table = None
-        if not per_pixel:
+        if not per_pixel and (on_device or not _ZERO_COPY):
             table = packing.observer_table(zl, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
-            if on_device or not _ZERO_COPY:
-                obs_dev = engine.upload_observers(table)
+            obs_dev = engine.upload_observers(table)
         if on_device:
             u_dev = unit_vectors.to(torch.float64).contiguous()
         else:
             if isinstance(unit_vectors, torch.Tensor):
-                u_host = unit_vectors.to(torch.float64).reshape(3, n).contiguous()
+                u_host = unit_vectors
+                if not (u_host.dtype == torch.float64 and u_host.dim() == 2 and u_host.is_contiguous()):
+                    u_host = u_host.to(torch.float64).reshape(3, n).contiguous()
             else:
                 u_host = torch.from_numpy(np.ascontiguousarray(np.asarray(unit_vectors, dtype=np.float64).reshape(3, n)))
             if not u_host.is_pinned():
                 u_host = u_host.pin_memory()
             if not per_pixel and _ZERO_COPY:
-                res = _zero_copy_call(zl, u_host, table, prec, return_comps, all_spec, out)
+                res = _zero_copy_call(zl, u_host, obs, earth, prec, return_comps, all_spec, out)
                 if res is not None:
                     return res
+                table = packing.observer_table(zl, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
                 obs_dev = engine.upload_observers(table)
             if not per_pixel and n >= 2 * _PIPE_CHUNK:
                 return _pipelined_host_call(zl, u_host, obs_dev, prec, return_comps, all_spec, out)
@@ -415,6 +418,8 @@ def _result_buffer(zl, n, return_comps, all_spec, out):
 
 
 _OBS_STAGING = threading.local()
+_CUTOFF_OFFSET = _lib.ZlModel.cutoff.offset
+_CUTOFF_SIZE = _lib.ZlModel.cutoff.size
 
 
 def _mapped_observers(table):
@@ -432,12 +437,30 @@ def _mapped_observers(table):
         t = torch.empty(max(raw.size, 4096), dtype=torch.uint8, pin_memory=True)
         buf = cache[dev] = (t, engine.mapped_pointer(t))
     buf[0].numpy()[: raw.size] = raw
+    _OBS_STAGING.key = None  # the staged record changed
     return buf[1]
 
 
-def _zero_copy_call(zl, u_host, table, prec, return_comps, all_spec, out):
+def _staged_observer(zl, obs, earth):
+    """Device address of this thread's staged record of one observer (_mapped_observers), rebuilt
+    only when the observer, Earth, the device or the model's cutoff spheres (which decide its
+    flags) differ from the thread's previous call: a repeated call skips building the record
+    (numpy, ctypes and zl_observer_flags) and staging it.  None if the buffer is unmapped."""
+    import torch
+
+    key = (torch.cuda.current_device(), obs.tobytes(), earth.tobytes(), zl.n_ranges,
+           ctypes.string_at(ctypes.addressof(zl) + _CUTOFF_OFFSET, _CUTOFF_SIZE))
+    if getattr(_OBS_STAGING, "key", None) == key:
+        return _OBS_STAGING.ptr
+    table = packing.observer_table(zl, obs, earth, np.zeros(1, dtype=np.int64), any_mode=False)
+    ptr = _mapped_observers(table)
+    _OBS_STAGING.key, _OBS_STAGING.ptr = (key, ptr) if ptr is not None else (None, None)
+    return ptr
+
+
+def _zero_copy_call(zl, u_host, obs, earth, prec, return_comps, all_spec, out):
     """One launch on mapped host memory (unit vectors, observer record and result); None when a
-    buffer is not device-addressable.  The staging buffer is reused only after the
+    buffer is not device-addressable.  The staging buffer is rewritten only after the
     synchronisation below, so calls of one thread never overwrite a record in use."""
     import torch
 
@@ -446,12 +469,14 @@ def _zero_copy_call(zl, u_host, table, prec, return_comps, all_spec, out):
     po = engine.mapped_pointer(host) if host.is_contiguous() else None
     if pu is None or po is None:
         return None
-    pobs = _mapped_observers(table)
+    pobs = _staged_observer(zl, obs, earth)
     if pobs is None:
         return None
-    engine.forward_ptr(zl, pu, u_host.shape[1], pobs, 1, prec, po if return_comps else None,
-                       None if return_comps else po)
-    torch.cuda.current_stream().synchronize()
+    stream = torch.cuda.current_stream()
+    rc = _lib.load().zl_forward(ctypes.byref(zl), pu, u_host.shape[1], pobs, 1, prec, po if return_comps else None,
+                                None if return_comps else po, stream.cuda_stream)
+    _lib.check(rc, "zl_forward")
+    stream.synchronize()
     return host if out is not None else host.numpy()
 
 
