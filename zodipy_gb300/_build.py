@@ -41,6 +41,14 @@ SOURCES = [
     "zl_tod.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Per-file code-generation flags, kept where they measured faster on GB300: ptxas's most
+# register-hungry scheduling took the Kelsall adjoint kernels 0.7-2.1 % faster (and the
+# forward kernels up to 4.6 % slower, so they keep the default).
+FILE_FLAGS = {
+    src: ["-Xptxas=--register-usage-level=10"]
+    for src in ("zl_bwd_f32_dirbe.cu", "zl_bwd_f32_dirbe34.cu", "zl_bwd_dirbe_cp.cu", "zl_bwd_dirbe_cp34.cu",
+                "zl_bwd_f32_planck.cu")
+}
 
 
 def nvcc_path() -> str:
@@ -77,7 +85,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc, *flags, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc, *flags, *FILE_FLAGS.get(src, []), "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         res = subprocess.run(cmd, capture_output=True, text=True)
