@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         for (int j = 0; j < 4; ++j) sC[j][s] = bc2(0.f);
       }
 
-#pragma unroll 1
+#pragma unroll(SCAT ? 2 : 1)  // two nodes per iteration with scattering: 1.6 % faster; without, 2.5 % slower
       for (int k = 0; k < P.n_nodes; ++k) {
         const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
         const float wk = P.gl_w[k];
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
 #pragma unroll
       for (int s = 0; s < NSPEC; ++s) bE[s] = bA[s] = bc2(0.f);
 
-#pragma unroll 1
+#pragma unroll(SCAT ? 2 : 1)  // two nodes per iteration with scattering: 1.6 % faster; without, 2.5 % slower
       for (int k = 0; k < P.n_nodes; ++k) {
         const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
         const float wk = P.gl_w[k];
