@@ -328,6 +328,10 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
       // With scattering the bands' share of the work is too small for the branches to pay.
       constexpr bool TAIL = !SCAT;
       int k12 = P.n_nodes, k3 = P.n_nodes;
+      // and the nodes at which bands 1 and 2 (and band 3, which reuses band 1's) evaluate the
+      // inner-cutoff factor 1 - e^-y and y e^-y / (1 - e^-y); at the others they are 1.0f and +0
+      // for every pixel of the warp, the same bits (cutoff_interval)
+      int2 r4 = make_int2(0, P.n_nodes);
       if (TAIL) {
         const float bt = B.beta_h.hi;
         const float b2h = fmaxf(fmaf(B.oxf, B.oxf, fmaf(B.oyf, B.oyf, B.ozf * B.ozf)) - bt * bt, 0.f);
@@ -337,6 +341,9 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
         };
         k12 = warp_tail_index(P, fmaxf(tail(C1), tail(C2)));
         k3 = warp_tail_index(P, tail(C3));
+        const float2 cut1 = cutoff_interval(h0, m0 + bt, b2h, K1.c[4]);
+        const float2 cut2 = cutoff_interval(h0, m0 + bt, b2h, K2.c[4]);
+        r4 = warp_node_range(P, fminf(cut1.x, cut2.x), fmaxf(cut1.y, cut2.y));
       }
 
       // bands 1 and 2: the scalar kernel's acc[off + j] per lane (before comp_pfactors)
@@ -372,21 +379,24 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
           const float2 lgx = lg2_2(x);
           const float2 xpv = mul2(x4, c2P);
           const float2 t3 = add2(bc2(1.f), xpv);
-          const float2 qq = mul2(bc2(N.R2), c4P);
-          const float2 qq2 = mul2(qq, qq), qq4 = mul2(qq2, qq2), qq8 = mul2(qq4, qq4);
-          const float2 y = mul2(qq8, qq2);
-          const float2 emy = ex2_2(mul2(bc2(-kLog2e), y));
-          // 1 - e^-y: its series below y = 1/4, the difference above
-          const float2 ny = mul2(y, bc2(-1.f));
-          float2 ser = fma2(ny, bc2(1.f / 720.f), bc2(1.f / 120.f));
-          ser = fma2(ny, ser, bc2(1.f / 24.f));
-          ser = fma2(ny, ser, bc2(1.f / 6.f));
-          ser = fma2(ny, ser, bc2(0.5f));
-          ser = mul2(y, fma2(ny, ser, bc2(1.f)));
-          const float2 om = sub2(bc2(1.f), emy);
-          const float2 t4 = make_float2(y.x < 0.25f ? ser.x : om.x, y.y < 0.25f ? ser.y : om.y);
-          const float2 ye = mul2(mul2(y, emy), make_float2(__fdividef(1.f, t4.x), __fdividef(1.f, t4.y)));
-          const float2 Y4 = make_float2(t4.x > 0.f ? ye.x : 1.f, t4.y > 0.f ? ye.y : 1.f);
+          float2 t4 = bc2(1.f), Y4 = bc2(0.f);
+          if (!TAIL || (k >= r4.x && k < r4.y)) {
+            const float2 qq = mul2(bc2(N.R2), c4P);
+            const float2 qq2 = mul2(qq, qq), qq4 = mul2(qq2, qq2), qq8 = mul2(qq4, qq4);
+            const float2 y = mul2(qq8, qq2);
+            const float2 emy = ex2_2(mul2(bc2(-kLog2e), y));
+            // 1 - e^-y: its series below y = 1/4, the difference above
+            const float2 ny = mul2(y, bc2(-1.f));
+            float2 ser = fma2(ny, bc2(1.f / 720.f), bc2(1.f / 120.f));
+            ser = fma2(ny, ser, bc2(1.f / 24.f));
+            ser = fma2(ny, ser, bc2(1.f / 6.f));
+            ser = fma2(ny, ser, bc2(0.5f));
+            ser = mul2(y, fma2(ny, ser, bc2(1.f)));
+            const float2 om = sub2(bc2(1.f), emy);
+            t4 = make_float2(y.x < 0.25f ? ser.x : om.x, y.y < 0.25f ? ser.y : om.y);
+            const float2 ye = mul2(mul2(y, emy), make_float2(__fdividef(1.f, t4.x), __fdividef(1.f, t4.y)));
+            Y4 = make_float2(t4.x > 0.f ? ye.x : 1.f, t4.y > 0.f ? ye.y : 1.f);
+          }
           t4s[C1] = t4.x;  // band 3's inner-cutoff term
           y4s[C1] = Y4.x;
           const float2 du = mul2(mul2(mul2(bc2(N.rinv), t2), t3), t4);
@@ -442,7 +452,14 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
 
         // ---- band 3 (band 1's inner-cutoff term; flushes the range's T_0 / delta sums)
         if (!TAIL || k < k3) {
-          if (TAIL && k >= k12) band1_cutoff(N.R2, K1.c[4], t4s[C1], y4s[C1]);
+          if (TAIL && k >= k12) {
+            if (k >= r4.x && k < r4.y) {
+              band1_cutoff(N.R2, K1.c[4], t4s[C1], y4s[C1]);
+            } else {
+              t4s[C1] = 1.f;
+              y4s[C1] = 0.f;
+            }
+          }
           const CompTerms t = comp_terms<LAYOUT, MASK, FLAGS>(C3, P, A, B, xk, N, t4s, y4s);
           comp_accumulate<LAYOUT, MASK, NSPEC, SCAT>(C3, P, A, B, wk, N, t, kpix, wq, fthx, fthy, acc);
         } else {

@@ -201,6 +201,53 @@ __device__ __forceinline__ int warp_tail_index(const KParamsF32& P, float xs) {
   return lo;
 }
 
+// Abscissa interval of the nodes at which a band's inner-cutoff factor 1 - e^-y, y = (R/delta_r)^20
+// (number_density.py:109), may differ from 1.0f: R < 1.26 delta_r.  Beyond it y > 101, e^-y
+// (ex2.approx.ftz of -y log2(e) < -126) is zero and 1 - e^-y is exactly 1.0f, as is the adjoint's
+// y e^-y / (1 - e^-y); 1 - e^-y rounds to 1.0f from R = 1.162 delta_r on, so the bound leaves 8 %
+// of R for the float32 rounding of this estimate.  R^2 = (h x + w)^2 + b2 along the line of sight
+// (h, w, b2: the pixel's set-up); returns (x1, x2), x1 > x2 when no point is that close.
+__device__ __forceinline__ float2 cutoff_interval(float h, float w, float b2, float inv_dr2) {
+  const float D = __fdividef(1.5876f, inv_dr2) - b2;  // (1.26 delta_r)^2 - b^2
+  if (!(D > 0.f)) return make_float2(INFINITY, -INFINITY);
+  const float sq = sqrtf(D);
+  if (!(h > 0.f)) return fabsf(w) < sq ? make_float2(-INFINITY, INFINITY) : make_float2(INFINITY, -INFINITY);
+  const float ih = __fdividef(1.f, h);
+  return make_float2((-w - sq) * ih, (sq - w) * ih);
+}
+
+// Order-preserving map of floats to unsigned integers (warp minima and maxima as integer ones).
+__device__ __forceinline__ uint32_t float_key(float x) {
+  const uint32_t b = __float_as_uint(x);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Node indices [lo, hi) covering the abscissa interval (x1, x2) of every active lane of the warp
+// (lo == hi: none).  Warp-uniform.
+__device__ __forceinline__ int2 warp_node_range(const KParamsF32& P, float x1, float x2) {
+  const uint32_t m = __activemask();
+  const float x1w = key_float(__reduce_min_sync(m, float_key(x1)));
+  const float x2w = key_float(__reduce_max_sync(m, float_key(x2)));
+  if (!(x1w <= x2w)) return make_int2(0, 0);
+  int lo = 0, hi = P.n_nodes;  // first node at or above x1w (nodes ascend in x)
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (P.gl_x_hi[mid] < x1w) lo = mid + 1;
+    else hi = mid;
+  }
+  const int first = lo;
+  hi = P.n_nodes;  // first node above x2w
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (P.gl_x_hi[mid] <= x2w) lo = mid + 1;
+    else hi = mid;
+  }
+  return make_int2(first, lo);
+}
+
 // Fan, comet, narrow and broad band of the RRM model (number_density.py:184-342) in float32,
 // without the amplitude C.c[0] (the caller applies it).
 // The radial mask R_inner <= |X - X_0| <= R_outer and the narrow band's cut |beta| < beta_nb are

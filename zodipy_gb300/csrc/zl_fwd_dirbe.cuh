@@ -108,6 +108,17 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
     };
     const int k12 = warp_tail_index(P, fmaxf(tail(1), tail(2)));
     const int k3 = warp_tail_index(P, tail(3));
+    // nodes at which bands 1 and 2 (and band 3, which reuses band 1's) evaluate their inner-cutoff
+    // factor 1 - e^-(R/delta_r)^20; at the others it is 1.0f for every pixel of the warp, the same
+    // bits (cutoff_interval).  Without scattering: 0.9 % faster; with it 0.4 % slower, so that
+    // instantiation evaluates the factor at every node
+    constexpr bool kCutAll = (FLAGS >> 1) & 1u;  // scattering: every node
+    int2 r4 = make_int2(0, P.n_nodes);
+    if (!kCutAll) {
+      const float2 cut1 = cutoff_interval(PS.hs[1].hi, PS.wm[1].hi, PS.b2[1], C1.c[4]);
+      const float2 cut2 = cutoff_interval(PS.hs[2].hi, PS.wm[2].hi, PS.b2[2], C2.c[4]);
+      r4 = warp_node_range(P, fminf(cut1.x, cut2.x), fmaxf(cut1.y, cut2.y));
+    }
 
     // quadrature sums per component (pairs in float2), blocks of kSumBlock nodes, Kahan across blocks
     float ps0[NSPEC], ps3[NSPEC], pS0[NSPEC], pS3[NSPEC], as0[NSPEC], ac0[NSPEC], as3[NSPEC], ac3[NSPEC];
@@ -172,9 +183,12 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
         const float2 z2 = mul2(zz, zz);
         const float2 t2 = ex2_2(mul2(bc2(-kLog2e), mul2(mul2(z2, z2), z2)));
         const float2 t3 = fma2(mul2(z2, z2), cpair(C1, C2, 2), bc2(1.f));
-        const float2 q = mul2(bc2(R2), cpair(C1, C2, 4));  // (R/delta_r)^2
-        const float2 q2 = mul2(q, q), q4 = mul2(q2, q2), q8 = mul2(q4, q4);
-        const float2 t4 = one_minus_emy2(mul2(q8, q2));
+        float2 t4 = bc2(1.f);
+        if (kCutAll || (k >= r4.x && k < r4.y)) {
+          const float2 q = mul2(bc2(R2), cpair(C1, C2, 4));  // (R/delta_r)^2
+          const float2 q2 = mul2(q, q), q4 = mul2(q2, q2), q8 = mul2(q4, q4);
+          t4 = one_minus_emy2(mul2(q8, q2));
+        }
         t4_band1 = t4.x;
         const float2 dens = mul2(mul2(mul2(bc2(rinv), t2), t3), t4);
 #pragma unroll
@@ -186,7 +200,7 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
 
       // ---- band 3 (inner-cutoff factor of band 1) -------------------------------
       if (k < k3) {
-        if (k >= k12) t4_band1 = one_minus_emy1(band_y1(R2, C1.c[4]));
+        if (k >= k12) t4_band1 = (kCutAll || (k >= r4.x && k < r4.y)) ? one_minus_emy1(band_y1(R2, C1.c[4])) : 1.f;
         const float Z = lin_ff(PS.z1[3], xk, PS.z0[3]);
         const float zz = Z * rinv * C3.c[1];  // only its square is used
         const float z2 = zz * zz;
