@@ -457,11 +457,12 @@ struct CompTerms {
   float du, GR, GZ, rcinv, p6, p7, p8, p9, p10, dthx, dthy;
 };
 
-// t4s / y4s: a band's 1 - e^-y and y d ln(1 - e^-y)/dy, reused by equal bands.
+// t4s / y4s: a band's 1 - e^-y and y d ln(1 - e^-y)/dy, reused by equal bands.  in4 false: the
+// node lies outside the warp's inner-cutoff range (cutoff_interval), where they are 1.0f and +0.
 template <uint32_t LAYOUT, uint32_t MASK, uint32_t FLAGS, int NC, int NSPEC>
 __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, const KGradAux& A,
                                                 const BwdPix<NC, NSPEC>& B, ff xk, const NodeR<NSPEC>& N,
-                                                float* t4s, float* y4s) {
+                                                float* t4s, float* y4s, bool in4 = true) {
   using L = Lay<LAYOUT>;
   using Fl = KFlags<FLAGS>;
   const KCompF32& C = P.comp[c];
@@ -525,7 +526,10 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
       Y4 = y4s[L::first_band(c)];
       shared = true;
     }
-    if (!shared) {
+    if (!shared && !in4) {
+      t4 = 1.f;
+      Y4 = 0.f;
+    } else if (!shared) {
       const float qq = Rc2 * C.c[4];
       const float qq2 = qq * qq, qq4 = qq2 * qq2, qq8 = qq4 * qq4;
       const float y = qq8 * qq2;
@@ -752,6 +756,20 @@ __device__ __forceinline__ void bwd_tile_reduce(const float (&acc)[NG], float (*
 // every group launch carries only its own accumulators; parameters shared by
 // all components (T_0, delta, C1..C3, S) are summed over the groups' partials.
 // SCAT: some component has a non-zero albedo (scattering terms are evaluated).
+// The scalar adjoint takes inner-cutoff ranges with compiled flags, no scattering and every band of
+// the launch centred on the Sun (the range is estimated from the range's heliocentric geometry).
+template <uint32_t LAYOUT, uint32_t MASK, uint32_t FLAGS, bool SCAT>
+__host__ __device__ constexpr bool kCutRanges() {
+  if (SCAT || FLAGS == kFlagsRuntime) return false;
+  bool any = false;
+  for (int c = 0; c < Lay<LAYOUT>::ncomp(); ++c)
+    if (((MASK >> c) & 1u) && Lay<LAYOUT>::type(c) == ZL_BAND) {
+      if ((FLAGS >> (8 + c)) & 1u) return false;
+      any = true;
+    }
+  return any;
+}
+
 template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
 __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ KParamsF32 P,
                                                         const __grid_constant__ KGradAux A,
@@ -791,11 +809,29 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       float kpix[NC];  // K = g em1 per component (one spectral set, no scattering)
 #pragma unroll
       for (int c = 0; c < NC; ++c) kpix[c] = KF ? B.gup[c][0] * P.spec[0].em1[c] : 0.f;
+      // nodes at which the bands' inner-cutoff factor and its log-derivative may differ from 1.0f
+      // and +0 for some pixel of the warp (compiled flags, bands centred on the Sun, no scattering)
+      int2 r4 = make_int2(0, P.n_nodes);
+      if (kCutRanges<LAYOUT, MASK, FLAGS, SCAT>()) {
+        const float bt = B.beta_h.hi;
+        const float b2h = fmaxf(fmaf(B.oxf, B.oxf, fmaf(B.oyf, B.oyf, B.ozf * B.ozf)) - bt * bt, 0.f);
+        float x1 = INFINITY, x2 = -INFINITY;
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+          if (((MASK >> c) & 1u) && L::type(c) == ZL_BAND) {
+            const int r = L::range(c);
+            const float2 iv = cutoff_interval(B.hs_r[r].hi, B.mid_r[r].hi + bt, b2h, P.comp[c].c[4]);
+            x1 = fminf(x1, iv.x);
+            x2 = fmaxf(x2, iv.y);
+          }
+        r4 = warp_node_range(P, x1, x2);
+      }
 
 #pragma unroll 1
       for (int k = 0; k < P.n_nodes; ++k) {
         const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
         const float wk = P.gl_w[k];
+        const bool in4 = k >= r4.x && k < r4.y;
         NodeR<NSPEC> N;
         float t4s[NC], y4s[NC];
 #pragma unroll
@@ -806,7 +842,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
           const int type = L::type(c);
           if (L::first(c))
             node_range<NSPEC, SCAT>(P, B, L::range(c), type == ZL_CLOUD || type == ZL_BAND, xk, tab_sm, nT, N);
-          const CompTerms t = comp_terms<LAYOUT, MASK, FLAGS>(c, P, A, B, xk, N, t4s, y4s);
+          const CompTerms t = comp_terms<LAYOUT, MASK, FLAGS>(c, P, A, B, xk, N, t4s, y4s, in4);
           comp_accumulate<LAYOUT, MASK, NSPEC, SCAT>(c, P, A, B, wk, N, t, kpix, wq, fthx, fthy, acc);
         }
       }
