@@ -25,6 +25,7 @@ SOURCES = [
     "zl_fwd_f32_dirbe.cu",
     "zl_fwd_f32_planck.cu",
     "zl_fwd_f32_generic.cu",
+    "zl_fwd_f32_rrm.cu",
     "zl_fwd_f32x2_dirbe.cu",
     "zl_fwd_f32x2_dirbe_scat.cu",
     "zl_fwd_f32x2_planck.cu",

@@ -183,9 +183,18 @@ void first_in_range(const ZlModel& m, int32_t* out) {
   for (int c = 0; c < m.n_comps; ++c) out[c] = (c == 0 || m.comp[c].range != m.comp[c - 1].range) ? 1 : 0;
 }
 
-// 1 = DIRBE-like (cloud | 3 bands on one range | ring | feature), 2 = Planck-like, 0 = generic
-// (every RRM model runs the generic layout)
+// 1 = DIRBE-like (cloud | 3 bands on one range | ring | feature), 2 = Planck-like, 3 = the
+// registry's RRM arrangement (Lay<kLayoutRRM>), 0 = generic
 int detect_layout(const ZlModel& m) {
+  if (m.family == ZL_RRM) {
+    static const int rrm_t[8] = {ZL_FAN, ZL_COMET, ZL_NARROW_BAND, ZL_NARROW_BAND, ZL_BROAD_BAND, ZL_INTERSTELLAR,
+                                 ZL_RING_RRM, ZL_FEATURE_RRM};
+    static const int rrm_r[8] = {0, 1, 2, 2, 2, 3, 4, 5};
+    if (m.n_comps != 8) return 0;
+    for (int c = 0; c < 8; ++c)
+      if (m.comp[c].type != rrm_t[c] || m.comp[c].range != rrm_r[c]) return 0;
+    return 3;
+  }
   if (m.family != ZL_KELSALL) return 0;
   int32_t first[ZL_MAX_COMPS];
   first_in_range(m, first);

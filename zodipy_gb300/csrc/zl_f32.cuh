@@ -14,6 +14,7 @@ constexpr uint32_t kLayoutGeneric = 0u;
 template <uint32_t LAYOUT>
 struct Lay {
   static constexpr bool generic = (LAYOUT == 0u);
+  static constexpr bool rrm = false;  // grain temperature per component (ZL_RRM), not shared
   __host__ __device__ static constexpr int ncomp() {
     if (generic) return ZL_MAX_COMPS;
     int n = 0;
@@ -36,6 +37,26 @@ struct Lay {
       if (range(j) == range(c) && type(j) == ZL_BAND) return j;
     return c;
   }
+};
+
+// The registry's RRM model (zodipy/model_registry.py:64-73, rrm-experimental): fan | comet |
+// narrow band, narrow band, broad band (one LOS range) | interstellar | ring | feature.  Its
+// component types and LOS ranges are compiled in; every parameter (offsets, scattering) is read
+// at run time (kFlagsRuntime), and each component has its own grain temperature law.
+constexpr uint32_t kLayoutRRM = 0x80000000u;
+
+template <>
+struct Lay<kLayoutRRM> {
+  static constexpr bool generic = false;
+  static constexpr bool rrm = true;
+  __host__ __device__ static constexpr int ncomp() { return 8; }
+  __host__ __device__ static constexpr int type(int c) {
+    return c == 0 ? ZL_FAN : c == 1 ? ZL_COMET : c <= 3 ? ZL_NARROW_BAND : c == 4 ? ZL_BROAD_BAND
+         : c == 5 ? ZL_INTERSTELLAR : c == 6 ? ZL_RING_RRM : ZL_FEATURE_RRM;
+  }
+  __host__ __device__ static constexpr int range(int c) { return c <= 1 ? c : c <= 4 ? 2 : c - 2; }
+  __host__ __device__ static constexpr bool first(int c) { return c == 0 || range(c) != range(c - 1); }
+  __host__ __device__ static constexpr int first_band(int c) { return c; }
 };
 
 // Compile-time properties of a model for the built-in layouts (FLAGS); bit 0 set = read them

@@ -8,7 +8,7 @@ namespace zl {
 // Compile-time flag set of a model for the layout kernels (see KFlags), or kFlagsRuntime when
 // the model's pattern is not one the layouts are compiled for.
 uint32_t f32_flags(const KParamsF32& P, int layout) {
-  if (layout == 0) return kFlagsRuntime;
+  if (layout == 0 || layout == 3) return kFlagsRuntime;
   uint32_t f = P.has_scat ? 2u : 0u;
   for (int c = 0; c < P.n_comps; ++c) {
     const KCompF32& K = P.comp[c];
@@ -46,6 +46,7 @@ cudaError_t launch_fwd_f32(const KParamsF32& P, int layout, int kernel, bool tai
   }
   if (layout == 1) return launch_fwd_f32_dirbe(P, flags, plain_geometry, u, n, obs, oc, ot, st, L);
   if (layout == 2) return launch_fwd_f32_planck(P, flags, u, n, obs, oc, ot, st, L);
+  if (layout == 3 && !plain_geometry) return launch_fwd_f32_rrm(P, u, n, obs, oc, ot, st, L);
   return launch_fwd_f32_generic(P, u, n, obs, oc, ot, st, L);
 }
 

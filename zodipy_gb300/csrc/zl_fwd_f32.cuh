@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
   extern __shared__ float4 tab_sm[];  // [NSPEC][nT]
   // the observer set-up the block's pixels share; not for the generic layout (the RRM model),
   // which measured 1.6 % slower with it (its eight components' set-up in shared memory)
-  constexpr bool kShared = !L::generic;
+  constexpr bool kShared = !L::generic && !L::rrm;
   __shared__ ObsSetupF32<NC> s_obs;
   const int nT = P.n_temps;
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
@@ -498,7 +498,8 @@ __global__ void __launch_bounds__(128) fwd_f32_kernel(const __grid_constant__ KP
           if (type == ZL_CLOUD || type == ZL_BAND || masked(type)) rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
           R = R2 * rinv;
           lg2R = lg2_ftz(R);
-          const float T = (L::generic ? C.T0 : P.T0) * ex2_ftz((L::generic ? C.neg_delta : P.neg_delta) * lg2R);  // blackbody.py:16-30
+          const float T = (L::generic || L::rrm ? C.T0 : P.T0) *
+                          ex2_ftz((L::generic || L::rrm ? C.neg_delta : P.neg_delta) * lg2R);  // blackbody.py:16-30
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) wB[s] = wk * bb_lookup(tab_sm + s * nT, T, P.t_min, P.t_max, P.inv_dt, nT);
           if (Fl::scat(P)) {  // scattering.py:11-59
@@ -648,5 +649,7 @@ cudaError_t launch_fwd_f32_planck(const KParamsF32& P, uint32_t flags, const dou
                                   double* oc, double* ot, cudaStream_t st, const LaunchArgs& L);
 cudaError_t launch_fwd_f32_generic(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
                                    double* ot, cudaStream_t st, const LaunchArgs& L);
+cudaError_t launch_fwd_f32_rrm(const KParamsF32& P, const double* u, int64_t n, const ObsArgs& obs, double* oc,
+                               double* ot, cudaStream_t st, const LaunchArgs& L);
 
 }  // namespace zl
