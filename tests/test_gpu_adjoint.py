@@ -131,7 +131,10 @@ def test_adjoint_deterministic_across_launch_shapes(lib):
 def test_adjoint_fused_equals_sum_of_single_bands(lib):
     """A two-band launch gives the sum of the single-band gradients for shared parameters
     (to float32 accumulation accuracy: the fused pass forms sum_s g_s e_s per node) and
-    each band's own block for the spectral ones."""
+    each band's own block for the spectral ones.  The single-band launch forms the emissivity
+    and albedo sums from the density sum (sum w n B = n_0 sum w (n / n_0) B), the fused one
+    per set, so those agree to float32 rounding of each pixel's terms: the bound is 1e-6 of
+    the sum of the terms' magnitudes, the gradient for |g| (every term of one sign)."""
     import torch
 
     from zodipy_gb300 import engine, packing
@@ -140,21 +143,24 @@ def test_adjoint_fused_equals_sum_of_single_bands(lib):
     n = adj.u.shape[1]
     g = torch.randn((2, n), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(2))
     fused = engine.backward(zl, adj.u, adj.obs_dev, 1, g_total=g).cpu().numpy()
-    singles = []
+    singles, mags = [], []
     for s in range(2):
         m1 = type(zl).from_buffer_copy(zl)
         m1.n_spec = 1
         m1.spec[0] = zl.spec[s]
         tab = packing.observer_table(m1, [0.9833, 0, 0], [-0.17, 0.97, 0.0], [0], any_mode=False)
         obs1 = engine.upload_observers(tab)
-        singles.append(engine.backward(m1, adj.u, obs1, 1, g_total=g[s : s + 1].contiguous()).cpu().numpy())
+        gs = g[s : s + 1].contiguous()
+        singles.append(engine.backward(m1, adj.u, obs1, 1, g_total=gs).cpu().numpy())
+        mags.append(np.abs(engine.backward(m1, adj.u, obs1, 1, g_total=gs.abs()).cpu().numpy()))
     n_shared = fused.size - 2 * (2 * zl.n_comps + 4)
     summed = singles[0][:n_shared] + singles[1][:n_shared]
     scale = np.abs(singles[0][:n_shared]) + np.abs(singles[1][:n_shared])
     assert np.all(np.abs(fused[:n_shared] - summed) <= 1e-5 * scale + 1e-7 * scale.max())
     per = 2 * zl.n_comps + 4
-    np.testing.assert_allclose(fused[n_shared : n_shared + per], singles[0][n_shared:], rtol=1e-6, atol=1e-12)
-    np.testing.assert_allclose(fused[n_shared + per :], singles[1][n_shared:], rtol=1e-6, atol=1e-12)
+    for s, block in enumerate((fused[n_shared : n_shared + per], fused[n_shared + per :])):
+        ref, mag = singles[s][n_shared:], mags[s][n_shared:]
+        assert np.all(np.abs(block - ref) <= 1e-6 * mag + 1e-12), (s, np.max(np.abs(block - ref) / (mag + 1e-30)))
 
 
 def test_adjoint_component_and_total_upstream_agree(lib):

@@ -53,10 +53,11 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
   static_assert(((FLAGS >> (8 + CR)) & 3u) == 0u, "ring and feature centred on the Sun");
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
+  __shared__ int used_sm[NG];
   __shared__ BwdObs<NC> s_obs;  // the observer set-up the block's pixels share
   const int cached = bwd_obs_cache_index(OA, (int64_t)blockIdx.x * kTile, n_pix);
   if (threadIdx.x == 0 && cached >= 0) bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, record_observer(OA, cached), s_obs);
-  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);  // its barrier also publishes s_obs
+  bwd_block_init<LAYOUT, MASK, NSPEC, SCAT>(P, tab_sm, red_sm, used_sm);  // its barrier also publishes s_obs
   const int nT = P.n_temps;
   const KCompF32& Cf = P.comp[CF];
 
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         sD = fma2(mul2(wq, T), lg2R, sD);
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
-          sE[s] = fma2(wd, Bv[s], sE[s]);
+          if (!KF) sE[s] = fma2(wd, Bv[s], sE[s]);  // with KF, n_0 s5 (bwd_finalize)
           if (SCAT) {
             const KSpecF32& S = P.spec[s];
             sA[s] = fma2(wd, sf[s], sA[s]);
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
       fthx[CF] = fx, fthy[CF] = fy;
       bwd_finalize<LAYOUT, MASK, NSPEC, SCAT>(P, A, B, kpix, fthx, fthy, acc);
     }
-    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, partials, tile);
+    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, used_sm, partials, tile);
   }
 }
 
@@ -283,10 +284,11 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
                 "bands 1 and 2 centred on the Sun, with p = 4 and their own inner-cutoff terms");
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
+  __shared__ int used_sm[NG];
   __shared__ BwdObs<NC> s_obs;  // the observer set-up the block's pixels share
   const int cached = bwd_obs_cache_index(OA, (int64_t)blockIdx.x * kTile, n_pix);
   if (threadIdx.x == 0 && cached >= 0) bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, record_observer(OA, cached), s_obs);
-  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);  // its barrier also publishes s_obs
+  bwd_block_init<LAYOUT, MASK, NSPEC, SCAT>(P, tab_sm, red_sm, used_sm);  // its barrier also publishes s_obs
   const int nT = P.n_temps;
   const KCompF32& K1 = P.comp[C1];
   const KCompF32& K2 = P.comp[C2];
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
           wq += wqp.x + wqp.y;
 #pragma unroll
           for (int s = 0; s < NSPEC; ++s) {
-            bE[s] = fma2(wd, bc2(N.Bv[s]), bE[s]);
+            if (!KF) bE[s] = fma2(wd, bc2(N.Bv[s]), bE[s]);  // with KF, n_0 b5 (bwd_finalize)
             if (SCAT) {
               const KSpecF32& S = P.spec[s];
               bA[s] = fma2(wd, bc2(N.sf[s]), bA[s]);
@@ -484,7 +486,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
       }
       bwd_finalize<LAYOUT, MASK, NSPEC, SCAT>(P, A, B, kpix, fthx, fthy, acc);
     }
-    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, partials, tile);
+    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, used_sm, partials, tile);
   }
 }
 

@@ -640,7 +640,8 @@ __device__ __forceinline__ void comp_accumulate(int c, const KParamsF32& P, cons
   for (int s = 0; s < NSPEC; ++s) {
     const KSpecF32& S = P.spec[s];
     // per node only sum w n B and w n S_flux; the pixel's constant factors follow the loop
-    acc[G::eps(c, s)] = fmaf(wd, N.Bv[s], acc[G::eps(c, s)]);
+    // (with KF, sum w n B = n_0 acc[o + 5]: bwd_finalize forms it from that sum)
+    if (!KF) acc[G::eps(c, s)] = fmaf(wd, N.Bv[s], acc[G::eps(c, s)]);
     if (SCAT) acc[G::alb(c, s)] = fmaf(wd, N.sf[s], acc[G::alb(c, s)]);
     if (SCAT) {
       const float wg = wd * B.gup[c][s];
@@ -691,7 +692,8 @@ __device__ __forceinline__ void bwd_finalize(const KParamsF32& P, const KGradAux
     }
 #pragma unroll
     for (int s = 0; s < NSPEC; ++s) {
-      const float sB = acc[G::eps(c, s)], sS = SCAT ? acc[G::alb(c, s)] : 0.f;
+      // sum w n B: with KF it is n_0 sum w (n / n_0) B, the node sum acc[o + 5] (not yet scaled)
+      const float sB = KF ? A.n0[c] * acc[o + 5] : acc[G::eps(c, s)], sS = SCAT ? acc[G::alb(c, s)] : 0.f;
       acc[G::eps(c, s)] = B.gup[c][s] * A.one_m_alb[s][c] * sB;
       acc[G::alb(c, s)] = B.gup[c][s] * fmaf(-A.eps[s][c], sB, sS);
     }
@@ -718,28 +720,75 @@ __device__ __forceinline__ void bwd_finalize(const KParamsF32& P, const KGradAux
   }
 }
 
+// The entries of the gradient vector a launch writes (grad_used), in order, as a
+// compile-time list: the tile reduction's slots.
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT>
+struct UsedGrads {
+  static constexpr int NG = GradLay<LAYOUT, NSPEC>::NG;
+  int idx[NG];
+  int n;
+  __host__ __device__ constexpr UsedGrads() : idx{}, n(0) {
+    for (int j = 0; j < NG; ++j)
+      if (grad_used<LAYOUT, MASK, NSPEC, SCAT>(j)) idx[n++] = j;
+  }
+};
+
 // Block start: the blackbody tables into shared memory; the reduction rows zeroed
-// (entries the launch never writes stay zero).
-template <int NSPEC, int NG>
-__device__ __forceinline__ void bwd_block_init(const KParamsF32& P, float4* tab_sm, float (*red_sm)[NG]) {
+// (entries the launch never writes stay zero); the list of written entries (used_sm).
+template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, int NG>
+__device__ __forceinline__ void bwd_block_init(const KParamsF32& P, float4* tab_sm, float (*red_sm)[NG],
+                                               int* used_sm) {
+  constexpr UsedGrads<LAYOUT, MASK, NSPEC, SCAT> U{};
   const int nT = P.n_temps;
   for (int t = threadIdx.x; t < nT * NSPEC; t += blockDim.x) tab_sm[t] = P.table[t / nT][t % nT];
   for (int t = threadIdx.x; t < (kTile / 32) * NG; t += blockDim.x) red_sm[t / NG][t % NG] = 0.f;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int t = 0; t < U.n; ++t) used_sm[t] = U.idx[t];
+  }
   __syncthreads();
 }
 
-// Tile reduction: a fixed shuffle tree per written entry, then the warps in order.
+// One level of the warp's transposed reduction: each lane holds 2H partial sums; the lanes with
+// (lane & M) keep the upper H, the others the lower H, and each adds its partner's copy of the
+// slots it keeps (one shuffle per kept slot instead of one per slot and level).  Slot j's
+// partner slot H + j is padding on every lane when H + j >= K: then only the lower lane's sum
+// is needed, and the upper lane's (a padding slot) is left as whatever it adds up to.
+template <int M, int H, int K>
+__device__ __forceinline__ void warp_halve(float* v, bool up) {
+#pragma unroll
+  for (int j = 0; j < H; ++j) {
+    if (H + j >= K) {
+      v[j] += __shfl_xor_sync(0xffffffffu, v[j], M);
+    } else {
+      const float send = up ? v[j] : v[H + j];
+      const float keep = up ? v[H + j] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, M);
+    }
+  }
+}
+
+// Tile reduction: the written entries, packed into 32 W slots per lane, summed over the warp by
+// recursive halving (lane L ends with the warp's sums of slots L W .. L W + W - 1), then the
+// warps in order.
 template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, int NG>
-__device__ __forceinline__ void bwd_tile_reduce(const float (&acc)[NG], float (*red_sm)[NG],
+__device__ __forceinline__ void bwd_tile_reduce(const float (&acc)[NG], float (*red_sm)[NG], const int* used_sm,
                                                 double* __restrict__ partials, int64_t tile) {
+  constexpr UsedGrads<LAYOUT, MASK, NSPEC, SCAT> U{};
+  constexpr int K = U.n, W = (K + 31) / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float v[32 * W];
 #pragma unroll
-  for (int j = 0; j < NG; ++j) {
-    if (!grad_used<LAYOUT, MASK, NSPEC, SCAT>(j)) continue;
-    float v = acc[j];
+  for (int t = 0; t < 32 * W; ++t) v[t] = t < K ? acc[U.idx[t]] : 0.f;
+  warp_halve<16, 16 * W, K>(v, lane & 16);
+  warp_halve<8, 8 * W, K>(v, lane & 8);
+  warp_halve<4, 4 * W, K>(v, lane & 4);
+  warp_halve<2, 2 * W, K>(v, lane & 2);
+  warp_halve<1, W, K>(v, lane & 1);
 #pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-    if (lane == 0) red_sm[warp][j] = v;
+  for (int t = 0; t < W; ++t) {
+    const int g = lane * W + t;
+    if (g < K) red_sm[warp][used_sm[g]] = v[t];
   }
   __syncthreads();
   for (int j = threadIdx.x; j < NG; j += blockDim.x) {
@@ -785,10 +834,11 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
   constexpr int NG = G::NG;
   __shared__ float4 tab_sm[NSPEC * ZL_MAX_TEMPS];
   __shared__ float red_sm[kTile / 32][NG];
+  __shared__ int used_sm[NG];
   __shared__ BwdObs<NC> s_obs;  // the observer set-up the block's pixels share
   const int cached = bwd_obs_cache_index(OA, (int64_t)blockIdx.x * kTile, n_pix);
   if (threadIdx.x == 0 && cached >= 0) bwd_obs_setup<LAYOUT, MASK, FLAGS>(P, record_observer(OA, cached), s_obs);
-  bwd_block_init<NSPEC, NG>(P, tab_sm, red_sm);  // its barrier also publishes s_obs
+  bwd_block_init<LAYOUT, MASK, NSPEC, SCAT>(P, tab_sm, red_sm, used_sm);  // its barrier also publishes s_obs
   const int nT = P.n_temps;
 
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
@@ -848,7 +898,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       }
       bwd_finalize<LAYOUT, MASK, NSPEC, SCAT>(P, A, B, kpix, fthx, fthy, acc);
     }
-    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, partials, tile);
+    bwd_tile_reduce<LAYOUT, MASK, NSPEC, SCAT>(acc, red_sm, used_sm, partials, tile);
   }
 }
 
