@@ -110,10 +110,8 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         const float wk = P.gl_w[k];
         // ---- each lane's LOS range: position, distance, temperature -----------
         const float2 Rl = lin_ff_x2(hsP, xk, mdP);
-        const float2 X0 = fma2(Rl, bc2(B.uxf), bc2(B.oxf));
-        const float2 X1 = fma2(Rl, bc2(B.uyf), bc2(B.oyf));
-        const float2 X2 = fma2(Rl, bc2(B.uzf), bc2(B.ozf));
-        const float2 R2 = fma2(X0, X0, fma2(X1, X1, mul2(X2, X2)));
+        const float2 wl = add2(Rl, bc2(B.beta_h.hi));  // |X|^2 = w^2 + b^2 (node_range)
+        const float2 R2 = fma2(wl, wl, bc2(B.b2h));
         const float2 rinv = rsqrt_2(R2);
         const float2 R = mul2(R2, rinv);
         const float2 lg2R = lg2_2(R);
@@ -156,7 +154,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_rf_kernel(const __grid_consta
         const float dth2 = dth * dth;
         arg.y = fmaf(dth2, A.q[CF][5], arg.y);
         const float gth = -2.f * dth * A.q[CF][5];  // d ln n / d dtheta
-        const float Xc0 = X0.y - Cf.ox, Xc1 = X1.y - Cf.oy;
+        const float Xc0 = fmaf(Rl.y, B.uxf, B.oxf - Cf.ox), Xc1 = fmaf(Rl.y, B.uyf, B.oyf - Cf.oy);  // X - X_0
         const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
         const float dthx = gth * (Xc1 * rr - B.eqx[CF]), dthy = gth * (-Xc0 * rr - B.eqy[CF]);
         const float2 du = ex2_2(mul2(bc2(-kLog2e), arg));
@@ -335,8 +333,7 @@ __global__ void __launch_bounds__(kTile) bwd_dirbe_cb_kernel(const __grid_consta
       // for every pixel of the warp, the same bits (cutoff_interval)
       int2 r4 = make_int2(0, P.n_nodes);
       if (TAIL) {
-        const float bt = B.beta_h.hi;
-        const float b2h = fmaxf(fmaf(B.oxf, B.oxf, fmaf(B.oyf, B.oyf, B.ozf * B.ozf)) - bt * bt, 0.f);
+        const float bt = B.beta_h.hi, b2h = B.b2h;
         const float h0 = B.hs_r[0].hi, m0 = B.mid_r[0].hi;
         auto tail = [&](int c) {
           return band_zero_tail(B.un_c[c] * h0, fmaf(B.un_c[c], m0, B.on_c[c]), h0, m0 + bt, b2h, P.comp[c].c[1]);

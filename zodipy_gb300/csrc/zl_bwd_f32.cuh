@@ -92,6 +92,10 @@ struct BwdPix {
   ff hs_r[ZL_MAX_RANGES], mid_r[ZL_MAX_RANGES];  // (stop - start)/2 and (stop + start)/2 per LOS range
   ff beta_h;                                     // obs . u
   float uxf, uyf, uzf, oxf, oyf, ozf, bperp;
+  // squared impact parameters: |X|^2 = (R_los + obs . u)^2 + b2h about the Sun, and
+  // |X - X_0|^2 = (R_los + bc)^2 + b2c about an offset component's centre (bc = (obs - X_0) . u)
+  float b2h;
+  float bc[NC], b2c[NC];
   float un_c[NC], on_c[NC];                      // u . n_c and (obs - X_0,c) . n_c
   float rux[NC], ruy[NC], rox[NC], roy[NC];      // the feature's rotated u and obs - X_0
   float eqx[NC], eqy[NC];                        // d atan2(E - X_0) / d x_0, d y_0
@@ -100,116 +104,10 @@ struct BwdPix {
   float rr_c[NC];
 };
 
-// Pixel set-up (as the forward kernel) for the components in MASK.
-template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
-__device__ __forceinline__ void bwd_pixel_setup(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
-                                                const ObsArgs& OA, const double* __restrict__ g_comps,
-                                                const double* __restrict__ g_total, int64_t i,
-                                                BwdPix<Lay<LAYOUT>::ncomp(), NSPEC>& B) {
-  using L = Lay<LAYOUT>;
-  using Fl = KFlags<FLAGS>;
-  constexpr int NC = L::ncomp();
-  const int nr = P.n_ranges;
-  // as the forward's pixel_setup: doubles split by bit operations, fast float-float sums
-  const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
-  const PixObs O = pixel_observer(OA, i, n_pix);
-  const ff ox = ff_split(O.ox), oy = ff_split(O.oy), oz = ff_split(O.oz);
-  const uint32_t outside = O.outside;
-  B.uxf = ux.hi, B.uyf = uy.hi, B.uzf = uz.hi;
-  B.oxf = ox.hi, B.oyf = oy.hi, B.ozf = oz.hi;
-  const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
-  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
-  const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
-  B.beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));
-#pragma unroll
-  for (int r = 0; r < ZL_MAX_RANGES; ++r) {
-    bool used = false;
-#pragma unroll
-    for (int c = 0; c < NC; ++c) used = used || (((MASK >> c) & 1u) && L::range(c) == r);
-    if (used && r < nr) {
-      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
-                                                : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
-      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
-                                                    : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
-      B.hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
-      B.mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
-    } else {
-      B.hs_r[r] = B.mid_r[r] = ff{0.f, 0.f};
-    }
-  }
-  B.bperp = 0.f;
-  if (SCAT) {
-    const float cx = B.uyf * B.ozf - B.uzf * B.oyf, cy = B.uzf * B.oxf - B.uxf * B.ozf,
-                cz = B.uxf * B.oyf - B.uyf * B.oxf;
-    B.bperp = sqrtf(cx * cx + cy * cy + cz * cz);
-  }
-#pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    B.un_c[c] = B.on_c[c] = 0.f;
-#pragma unroll
-    for (int s = 0; s < NSPEC; ++s) B.gup[c][s] = 0.f;
-    B.wa_c[c] = B.wb_c[c] = ff{0.f, 0.f};
-    B.rr_c[c] = 0.f;
-    B.rux[c] = B.ruy[c] = B.rox[c] = B.roy[c] = B.eqx[c] = B.eqy[c] = 0.f;
-    if (!((MASK >> c) & 1u)) continue;
-    const KCompF32& C = P.comp[c];
-    const int type = L::type(c);
-    const ff hs = B.hs_r[L::range(c)], md = B.mid_r[L::range(c)];
-    const bool off = Fl::offset(C, c);
-    // X_obs - X_0 (exact for the components centred on the Sun; selecting X_obs for them
-    // instead raised the forward kernel's register count past five blocks per SM)
-    const ff dx = ff_add_fast(ox, ff{-C.ox, -C.ox_lo}), dy = ff_add_fast(oy, ff{-C.oy, -C.oy_lo}),
-             dz = ff_add_fast(oz, ff{-C.oz, -C.oz_lo});
-    if (c > 0 && ((MASK >> (c - 1)) & 1u) && C.same_plane_prev) {  // the ring's plane, for the feature
-      B.un_c[c] = B.un_c[c - 1];
-      B.on_c[c] = B.on_c[c - 1];
-    } else {
-      const ff nx = {C.nx, C.nx_lo}, ny = {C.ny, C.ny_lo}, nz = {C.nz, C.nz_lo};
-      const ff un = ff_add_fast(ff_add_fast(ff_mul_nr(ux, nx), ff_mul_nr(uy, ny)), ff_mul_nr(uz, nz));
-      const ff on = ff_add_fast(ff_add_fast(ff_mul_nr(dx, nx), ff_mul_nr(dy, ny)), ff_mul_nr(dz, nz));
-      B.un_c[c] = un.hi + un.lo;
-      B.on_c[c] = on.hi + on.lo;
-    }
-    // upstream gradient of this pixel, times (stop - start)/2: per component, or the total's
-    const float hsf = hs.hi + hs.lo;
-#pragma unroll
-    for (int s = 0; s < NSPEC; ++s)
-      B.gup[c][s] =
-          d2f_bits(g_comps ? g_comps[((int64_t)s * NC + c) * n_pix + i] : g_total[(int64_t)s * n_pix + i]) * hsf;
-    if (type == ZL_RING || type == ZL_FEATURE) {
-      const ff beta =
-          !off ? B.beta_h : ff_add_fast(ff_add_fast(ff_mul_nr(dx, ux), ff_mul_nr(dy, uy)), ff_mul_nr(dz, uz));
-      const ff d2 = !off ? r2 : ff_add_fast(ff_add_fast(ff_mul_nr(dx, dx), ff_mul_nr(dy, dy)), ff_mul_nr(dz, dz));
-      const ff wm = ff_add_fast(md, beta);
-      const ff cw = ff_add_fast(ff_add_fast(d2, ff_neg(ff_mul_nr(beta, beta))), ff_neg(ff{C.c[4], C.c[5]}));
-      const ff w0 = cw.hi < 0.f ? ff_sqrt(ff_neg(cw)) : ff{0.f, 0.f};
-      B.wa_c[c] = ff_add_fast(wm, ff_neg(w0));
-      B.wb_c[c] = ff_add_fast(wm, w0);
-      const ff res = ff_add_fast(ff_mul_nr(w0, w0), cw);
-      B.rr_c[c] = res.hi + res.lo;
-    }
-    if (type == ZL_FEATURE) {
-      const ff exf = ff_add_fast(ff_split(O.ex), ff{-C.ox, -C.ox_lo}), eyf = ff_add_fast(ff_split(O.ey), ff{-C.oy, -C.oy_lo});
-      const float ex = exf.hi + exf.lo, ey = eyf.hi + eyf.lo;
-      const float phi = atan2f(ey, ex) + C.c[6];
-      float sp, cp;
-      sincosf(phi, &sp, &cp);
-      const float ocx = dx.hi + dx.lo, ocy = dy.hi + dy.lo;
-      B.rux[c] = cp * B.uxf + sp * B.uyf;
-      B.ruy[c] = cp * B.uyf - sp * B.uxf;
-      B.rox[c] = cp * ocx + sp * ocy;
-      B.roy[c] = cp * ocy - sp * ocx;
-      const float e2 = ex * ex + ey * ey;
-      B.eqx[c] = ey / e2;   // d atan2(E - X_0)/d x_0
-      B.eqy[c] = -ex / e2;  // d atan2(E - X_0)/d y_0
-    }
-  }
-}
-
 // What the adjoint's pixel set-up derives from the observer (and Earth) alone, for the
 // components in MASK: shared by the pixels of a block that have the same observer
-// (bwd_obs_setup once per block, bwd_pixel_setup_obs per pixel).  The operations are those of
-// bwd_pixel_setup, so the bits are the same either way.
+// (bwd_obs_setup once per block, bwd_pixel_setup_obs per pixel; pixels of another observer
+// derive their own, bwd_obs_setup_own).
 template <int NC>
 struct BwdObs {
   ff ox, oy, oz, r2;
@@ -282,7 +180,7 @@ __device__ __forceinline__ void bwd_obs_setup(const KParamsF32& P, const PixObs&
   }
 }
 
-// Pixel i's adjoint set-up from its observer's (Q): bwd_pixel_setup's operations.
+// Pixel i's adjoint set-up from its observer's (Q), for the components in MASK.
 template <uint32_t LAYOUT, uint32_t MASK, int NSPEC, bool SCAT, uint32_t FLAGS>
 __device__ __forceinline__ void bwd_pixel_setup_obs(const KParamsF32& P, const double* __restrict__ u, int64_t n_pix,
                                                     const double* __restrict__ g_comps,
@@ -301,6 +199,9 @@ __device__ __forceinline__ void bwd_pixel_setup_obs(const KParamsF32& P, const d
   const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
   const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
   B.beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));
+  // |X_obs|^2 - (u . X_obs)^2 >= 0, as the forward forms it
+  const ff b2h_ff = ff_add(Q.r2, ff_neg(ff_mul(B.beta_h, B.beta_h)));
+  B.b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
 #pragma unroll
   for (int r = 0; r < ZL_MAX_RANGES; ++r) {
     bool used = false;
@@ -329,11 +230,19 @@ __device__ __forceinline__ void bwd_pixel_setup_obs(const KParamsF32& P, const d
     B.wa_c[c] = B.wb_c[c] = ff{0.f, 0.f};
     B.rr_c[c] = 0.f;
     B.rux[c] = B.ruy[c] = B.rox[c] = B.roy[c] = B.eqx[c] = B.eqy[c] = 0.f;
+    B.bc[c] = B.b2c[c] = 0.f;
     if (!((MASK >> c) & 1u)) continue;
     const KCompF32& C = P.comp[c];
     const int type = L::type(c);
     const ff hs = B.hs_r[L::range(c)], md = B.mid_r[L::range(c)];
     const bool off = Fl::offset(C, c);
+    if (off && !Fl::runtime) {  // (X_obs - X_0) . u and |X_obs - X_0|^2 - ((X_obs - X_0) . u)^2 >= 0
+      const ff dx = Q.dx[c], dy = Q.dy[c], dz = Q.dz[c];
+      const ff beta = ff_add_fast(ff_add_fast(ff_mul_nr(dx, ux), ff_mul_nr(dy, uy)), ff_mul_nr(dz, uz));
+      const ff bb = ff_add_fast(Q.d2[c], ff_neg(ff_mul_nr(beta, beta)));
+      B.bc[c] = beta.hi + beta.lo;
+      B.b2c[c] = fmaxf(bb.hi + bb.lo, 0.f);
+    }
     if (c > 0 && ((MASK >> (c - 1)) & 1u) && C.same_plane_prev) {  // the ring's plane, for the feature
       B.un_c[c] = B.un_c[c - 1];
     } else {
@@ -409,7 +318,7 @@ __device__ __forceinline__ int bwd_obs_cache_index(const ObsArgs& OA, int64_t fi
 // temperature, blackbody value and slope per spectral set, scattering terms.
 template <int NSPEC>
 struct NodeR {
-  float Rl, X0, X1, X2, R2, rinv, R, lg2R, Tn, T, flux, theta;
+  float Rl, R2, rinv, R, lg2R, Tn, T, flux, theta;
   float Bv[NSPEC], dB[NSPEC], sf[NSPEC], base[NSPEC], eC3[NSPEC];
 };
 
@@ -418,10 +327,8 @@ template <int NSPEC, bool SCAT, int NC>
 __device__ __forceinline__ void node_range(const KParamsF32& P, const BwdPix<NC, NSPEC>& B, int r, bool newton, ff xk,
                                            const float4* __restrict__ tab_sm, int nT, NodeR<NSPEC>& N) {
   N.Rl = node_position(B.hs_r[r], xk, B.mid_r[r]);
-  N.X0 = fmaf(N.Rl, B.uxf, B.oxf);
-  N.X1 = fmaf(N.Rl, B.uyf, B.oyf);
-  N.X2 = fmaf(N.Rl, B.uzf, B.ozf);
-  N.R2 = fmaf(N.X0, N.X0, fmaf(N.X1, N.X1, N.X2 * N.X2));
+  const float w = N.Rl + B.beta_h.hi;  // |X|^2 = w^2 + b^2 without forming X (no cancellation)
+  N.R2 = fmaf(w, w, B.b2h);
   N.rinv = rsqrt_ftz(N.R2);
   if (newton) N.rinv = N.rinv * fmaf(-0.5f * N.R2, N.rinv * N.rinv, 1.5f);
   N.R = N.R2 * N.rinv;
@@ -469,11 +376,17 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
   const int type = L::type(c);
   CompTerms t;
   t.p6 = t.p7 = t.p8 = t.p9 = t.p10 = t.dthx = t.dthy = 0.f;
-  // component frame: X - X_0, its norm, height above the symmetry plane
-  const float Xc0 = N.X0 - C.ox, Xc1 = N.X1 - C.oy, Xc2 = N.X2 - C.oz;
+  // component frame: |X - X_0|, height above the symmetry plane
   float Rc2 = N.R2, rcinv = N.rinv, Rc = N.R, lg2Rc = N.lg2R;
   if (Fl::offset(C, c)) {
-    Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
+    if (Fl::runtime) {  // any component may be offset: X - X_0 from the node position (fewer registers)
+      const float Xc0 = fmaf(N.Rl, B.uxf, B.oxf - C.ox), Xc1 = fmaf(N.Rl, B.uyf, B.oyf - C.oy),
+                  Xc2 = fmaf(N.Rl, B.uzf, B.ozf - C.oz);
+      Rc2 = fmaf(Xc0, Xc0, fmaf(Xc1, Xc1, Xc2 * Xc2));
+    } else {
+      const float wc = N.Rl + B.bc[c];
+      Rc2 = fmaf(wc, wc, B.b2c[c]);
+    }
     rcinv = rsqrt_ftz(Rc2);
     if (type == ZL_BAND) rcinv = rcinv * fmaf(-0.5f * Rc2, rcinv * rcinv, 1.5f);
     Rc = Rc2 * rcinv;
@@ -568,6 +481,7 @@ __device__ __forceinline__ CompTerms comp_terms(int c, const KParamsF32& P, cons
       const float gth = -2.f * dth * q[5];  // d ln n / d dtheta
       t.p9 = dth;                           // d/d theta = -gth pi/180 = 2 dth pi/180 / sigma_theta^2
       t.p10 = dth * dth;                    // d/d sigma_theta = 2 dth^2 / sigma_theta^3 per degree
+      const float Xc0 = fmaf(N.Rl, B.uxf, B.oxf - C.ox), Xc1 = fmaf(N.Rl, B.uyf, B.oyf - C.oy);  // X - X_0
       const float rr = __fdividef(1.f, Xc0 * Xc0 + Xc1 * Xc1);
       t.dthx = gth * (Xc1 * rr - B.eqx[c]);
       t.dthy = gth * (-Xc0 * rr - B.eqy[c]);
@@ -863,8 +777,7 @@ __global__ void __launch_bounds__(kTile) bwd_f32_kernel(const __grid_constant__ 
       // and +0 for some pixel of the warp (compiled flags, bands centred on the Sun, no scattering)
       int2 r4 = make_int2(0, P.n_nodes);
       if (kCutRanges<LAYOUT, MASK, FLAGS, SCAT>()) {
-        const float bt = B.beta_h.hi;
-        const float b2h = fmaxf(fmaf(B.oxf, B.oxf, fmaf(B.oyf, B.oyf, B.ozf * B.ozf)) - bt * bt, 0.f);
+        const float bt = B.beta_h.hi, b2h = B.b2h;
         float x1 = INFINITY, x2 = -INFINITY;
 #pragma unroll
         for (int c = 0; c < NC; ++c)
