@@ -129,9 +129,8 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
       ps12[s] = psq[s] = pS12[s] = pSq[s] = as12[s] = ac12[s] = asq[s] = acq[s] = bc2(0.f);
     }
 
-    // two nodes per iteration with scattering (1.5 % faster), one without (2 % faster)
-#pragma unroll(((FLAGS >> 1) & 1u) ? 2 : 1)
-    for (int k = 0; k < P.n_nodes; ++k) {
+    // one node: each component's term into its block sum
+    const auto node = [&](const int k) {
       const ff xk = {P.gl_x_hi[k], P.gl_x_lo[k]};
       const float wk = P.gl_w[k];
 
@@ -255,21 +254,37 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
           if (Fl::scat(P)) pSq[s] = fma2(wSq[s], dens, pSq[s]);
         }
       }
-
-      // ---- block sums into the compensated totals ------------------------------
-      if ((k % kSumBlock) == kSumBlock - 1 || k == P.n_nodes - 1) {
+    };
+    // the block sums into the compensated totals
+    const auto block_sum = [&]() {
 #pragma unroll
-        for (int s = 0; s < NSPEC; ++s) {
-          const KSpecF32& S = P.spec[s];
-          const float2 o12 = make_float2(S.outer[1], S.outer[2]), oq = make_float2(S.outer[4], S.outer[5]);
-          const float2 a12 = make_float2(S.outer_alb[1], S.outer_alb[2]), aq = make_float2(S.outer_alb[4], S.outer_alb[5]);
-          kahan_add(as0[s], ac0[s], Fl::scat(P) ? fmaf(ps0[s], S.outer[0], pS0[s] * S.outer_alb[0]) : ps0[s] * S.outer[0]);
-          kahan_add(as3[s], ac3[s], Fl::scat(P) ? fmaf(ps3[s], S.outer[3], pS3[s] * S.outer_alb[3]) : ps3[s] * S.outer[3]);
-          kahan_add2(as12[s], ac12[s], Fl::scat(P) ? fma2(ps12[s], o12, mul2(pS12[s], a12)) : mul2(ps12[s], o12));
-          kahan_add2(asq[s], acq[s], Fl::scat(P) ? fma2(psq[s], oq, mul2(pSq[s], aq)) : mul2(psq[s], oq));
-          ps0[s] = ps3[s] = pS0[s] = pS3[s] = 0.f;
-          ps12[s] = psq[s] = pS12[s] = pSq[s] = bc2(0.f);
-        }
+      for (int s = 0; s < NSPEC; ++s) {
+        const KSpecF32& S = P.spec[s];
+        const float2 o12 = make_float2(S.outer[1], S.outer[2]), oq = make_float2(S.outer[4], S.outer[5]);
+        const float2 a12 = make_float2(S.outer_alb[1], S.outer_alb[2]), aq = make_float2(S.outer_alb[4], S.outer_alb[5]);
+        kahan_add(as0[s], ac0[s], Fl::scat(P) ? fmaf(ps0[s], S.outer[0], pS0[s] * S.outer_alb[0]) : ps0[s] * S.outer[0]);
+        kahan_add(as3[s], ac3[s], Fl::scat(P) ? fmaf(ps3[s], S.outer[3], pS3[s] * S.outer_alb[3]) : ps3[s] * S.outer[3]);
+        kahan_add2(as12[s], ac12[s], Fl::scat(P) ? fma2(ps12[s], o12, mul2(pS12[s], a12)) : mul2(ps12[s], o12));
+        kahan_add2(asq[s], acq[s], Fl::scat(P) ? fma2(psq[s], oq, mul2(pSq[s], aq)) : mul2(psq[s], oq));
+        ps0[s] = ps3[s] = pS0[s] = pS3[s] = 0.f;
+        ps12[s] = psq[s] = pS12[s] = pSq[s] = bc2(0.f);
+      }
+    };
+    if (Fl::scat(P)) {  // a compile-time constant here
+      // with scattering: one loop over the nodes, two per iteration (1.5 % faster than one)
+#pragma unroll 2
+      for (int k = 0; k < P.n_nodes; ++k) {
+        node(k);
+        if ((k % kSumBlock) == kSumBlock - 1 || k == P.n_nodes - 1) block_sum();
+      }
+    } else {
+      // without: blocks of kSumBlock nodes, so no node tests for the end of its block (1.5 % faster
+      // than one loop with that test; with scattering 0.7 % slower)
+      for (int k0 = 0; k0 < P.n_nodes; k0 += kSumBlock) {
+        const int k1 = min(k0 + kSumBlock, P.n_nodes);
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k) node(k);
+        block_sum();
       }
     }
 
