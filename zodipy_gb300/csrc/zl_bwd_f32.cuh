@@ -197,10 +197,10 @@ __device__ __forceinline__ void bwd_pixel_setup_obs(const KParamsF32& P, const d
   B.uxf = ux.hi, B.uyf = uy.hi, B.uzf = uz.hi;
   B.oxf = ox.hi, B.oyf = oy.hi, B.ozf = oz.hi;
   const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
-  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
+  const ff b = ff_scale(ff_add_fast(oxux, oyuy), 2.0f);
   B.beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));
   // |X_obs|^2 - (u . X_obs)^2 >= 0, as the forward forms it
-  const ff b2h_ff = ff_add(Q.r2, ff_neg(ff_mul(B.beta_h, B.beta_h)));
+  const ff b2h_ff = ff_add_fast(Q.r2, ff_neg(ff_mul(B.beta_h, B.beta_h)));
   B.b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
 #pragma unroll
   for (int r = 0; r < ZL_MAX_RANGES; ++r) {
@@ -210,8 +210,8 @@ __device__ __forceinline__ void bwd_pixel_setup_obs(const KParamsF32& P, const d
     if (used && r < nr) {
       const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_in[r]);
       const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_out[r]);
-      B.hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
-      B.mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+      B.hs_r[r] = ff_scale(ff_add_fast(sp, ff_neg(st)), 0.5f);
+      B.mid_r[r] = ff_scale(ff_add_fast(sp, st), 0.5f);
     } else {
       B.hs_r[r] = B.mid_r[r] = ff{0.f, 0.f};
     }

@@ -129,14 +129,14 @@ __device__ __forceinline__ void pixel_setup_obs(const KParamsF32& P, const doubl
   const int nr = P.n_ranges;
   // float-float values of the doubles by bit operations (no float64 instruction); the sums
   // below are ff_add_fast (accurate to a few 2^-48 of their operands: the geometry needs
-  // absolute, not relative, accuracy), except where the cutoff spheres are intersected
+  // absolute, not relative, accuracy); only |X_obs|^2 - cutoff^2, per observer, is an exact sum
   const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
   const ff ox = Q.ox, oy = Q.oy, oz = Q.oz;
   const uint32_t outside = Q.outside;
   const float uxf = ux.hi, uyf = uy.hi;
 
   const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
-  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
+  const ff b = ff_scale(ff_add_fast(oxux, oyuy), 2.0f);
   const ff r2 = Q.r2;
   const ff beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));  // u . X_obs
 
@@ -146,8 +146,8 @@ __device__ __forceinline__ void pixel_setup_obs(const KParamsF32& P, const doubl
     if (r < nr) {
       const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_in[r]);
       const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_out[r]);
-      hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
-      mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+      hs_r[r] = ff_scale(ff_add_fast(sp, ff_neg(st)), 0.5f);
+      mid_r[r] = ff_scale(ff_add_fast(sp, st), 0.5f);
     } else {
       hs_r[r] = ff{0.f, 0.f};
       mid_r[r] = ff{0.f, 0.f};
@@ -155,7 +155,7 @@ __device__ __forceinline__ void pixel_setup_obs(const KParamsF32& P, const doubl
   }
 
   // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
-  const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
+  const ff b2h_ff = ff_add_fast(r2, ff_neg(ff_mul(beta_h, beta_h)));
   const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
   // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
   S.b2h = b2h;
@@ -244,7 +244,7 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   const int nr = P.n_ranges;
   // float-float values of the doubles by bit operations (no float64 instruction); the sums
   // below are ff_add_fast (accurate to a few 2^-48 of their operands: the geometry needs
-  // absolute, not relative, accuracy), except where the cutoff spheres are intersected
+  // absolute, not relative, accuracy); only |X_obs|^2 - cutoff^2, per observer, is an exact sum
   const ff ux = ff_split(u[i]), uy = ff_split(u[n_pix + i]), uz = ff_split(u[2 * n_pix + i]);
   const PixObs O = pixel_observer(OA, i, n_pix);
   const ff ox = ff_split(O.ox), oy = ff_split(O.oy), oz = ff_split(O.oz);
@@ -253,7 +253,7 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   const float oxf = ox.hi, oyf = oy.hi, ozf = oz.hi;
 
   const ff oxux = ff_mul_nr(ox, ux), oyuy = ff_mul_nr(oy, uy);
-  const ff b = ff_scale(ff_add(oxux, oyuy), 2.0f);
+  const ff b = ff_scale(ff_add_fast(oxux, oyuy), 2.0f);
   const ff r2 = ff_add(ff_add(ff_mul(ox, ox), ff_mul(oy, oy)), ff_mul(oz, oz));
   const ff beta_h = ff_add_fast(ff_add_fast(oxux, oyuy), ff_mul_nr(oz, uz));  // u . X_obs
 
@@ -265,8 +265,8 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
                                                 : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
       const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
                                                     : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
-      hs_r[r] = ff_scale(ff_add(sp, ff_neg(st)), 0.5f);
-      mid_r[r] = ff_scale(ff_add(sp, st), 0.5f);
+      hs_r[r] = ff_scale(ff_add_fast(sp, ff_neg(st)), 0.5f);
+      mid_r[r] = ff_scale(ff_add_fast(sp, st), 0.5f);
     } else {
       hs_r[r] = ff{0.f, 0.f};
       mid_r[r] = ff{0.f, 0.f};
@@ -274,7 +274,7 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   }
 
   // squared impact parameter of the line of sight about the Sun, |X_obs|^2 - (u . X_obs)^2 >= 0
-  const ff b2h_ff = ff_add(r2, ff_neg(ff_mul(beta_h, beta_h)));
+  const ff b2h_ff = ff_add_fast(r2, ff_neg(ff_mul(beta_h, beta_h)));
   const float b2h = fmaxf(b2h_ff.hi + b2h_ff.lo, 0.f);
   // scattering angle pi - atan2(|u x X_obs|, R_los + u . X_obs) (scattering.py:26-31)
   S.b2h = b2h;
