@@ -226,8 +226,10 @@ __device__ __forceinline__ ff ff_mul_nr(ff a, ff b) {
   return {p, e};
 }
 
-// sqrt of a positive float-float (one Newton correction of the FP32 root)
-__device__ __forceinline__ ff ff_sqrt(ff a) {
+// sqrt of a positive float-float (one Newton correction of the FP32 root), the residual
+// a - s^2 as a float-float sum; ff_div_ieee: a / b from IEEE divisions.  Kept for the Planck
+// layout's kernels, where the shorter forms below measured slower (different schedules).
+__device__ __forceinline__ ff ff_sqrt_sum(ff a) {
   if (!(a.hi > 0.f)) return {sqrtf(a.hi), 0.f};
   float r = rsqrtf(a.hi);
   float s = a.hi * r;
@@ -236,12 +238,37 @@ __device__ __forceinline__ ff ff_sqrt(ff a) {
   return ff_quick(s, d.hi * 0.5f * r);
 }
 
-// a / b (one Newton correction)
-__device__ __forceinline__ ff ff_div(ff a, ff b) {
+__device__ __forceinline__ ff ff_div_ieee(ff a, ff b) {
   float q = a.hi / b.hi;
   ff p = ff_mulf(b, q);
   ff r = ff_add(a, ff_neg(p));
   return ff_quick(q, r.hi / b.hi);
+}
+
+// sqrt of a positive float-float (one Newton correction of the FP32 root).  The root s is
+// within a few ulps of sqrt(a.hi), so s^2 = p + pe (exact, by an FMA) lies within a factor 2 of
+// a.hi and a.hi - p is exact (Sterbenz): the residual a - s^2 takes three additions.
+__device__ __forceinline__ ff ff_sqrt(ff a) {
+  if (!(a.hi > 0.f)) return {sqrtf(a.hi), 0.f};
+  const float r = rsqrtf(a.hi);
+  const float s = a.hi * r;
+  const float p = s * s, pe = fmaf(s, s, -p);
+  const float d = ((a.hi - p) - pe) + a.lo;
+  return ff_quick(s, d * 0.5f * r);
+}
+
+// a / b (one Newton correction).  q = a.hi / b.hi to a few ulps (reciprocal approximation), so
+// b.hi q = p + pe (exact, by an FMA) lies within a factor 2 of a.hi and a.hi - p is exact
+// (Sterbenz): the residual a - b q takes three additions and the low part's product.  Relative
+// error below 2^-42 (the reciprocal's error times the residual's; 2^-45 with IEEE divisions, at
+// four times the instructions).  A zero divisor gives an infinite or NaN quotient, as the
+// division does.
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float rb = __fdividef(1.f, b.hi);
+  const float q = a.hi * rb;
+  const float p = b.hi * q, pe = fmaf(b.hi, q, -p);
+  const float r = fmaf(-b.lo, q, ((a.hi - p) - pe) + a.lo);
+  return ff_quick(q, r * rb);
 }
 
 // Single MUFU instructions (flush-to-zero): the integrands never need subnormal

@@ -94,17 +94,20 @@ uint32_t f32_flags(const KParamsF32& P, int layout);
 // c = |X_obs|^2 - cutoff^2 is formed exactly (it cancels for an observer near the sphere;
 // sphere_distance_ff below, or once per observer); the other sums need accuracy relative to
 // their operands only (ff_add_fast).
+// SHORT: ff_sqrt and ff_div (three-addition residuals), else ff_sqrt_sum and ff_div_ieee.
+template <bool SHORT = true>
 __device__ __forceinline__ ff sphere_distance_ffc(ff b, ff c) {
   const ff D = ff_add_fast(ff_mul(b, b), ff_scale(c, -4.0f));
-  const ff sq = ff_sqrt(D);
+  const ff sq = SHORT ? ff_sqrt(D) : ff_sqrt_sum(D);
   const ff q = ff_scale(ff_add_fast(b, (b.hi < 0.f || (b.hi == 0.f && signbit(b.hi))) ? ff_neg(sq) : sq), -0.5f);
-  const ff cq = ff_div(c, q);
+  const ff cq = SHORT ? ff_div(c, q) : ff_div_ieee(c, q);
   if (isnan(q.hi) || isnan(cq.hi)) return {q.hi + cq.hi, 0.f};
   return (q.hi > cq.hi || (q.hi == cq.hi && q.lo >= cq.lo)) ? q : cq;
 }
 
+template <bool SHORT = true>
 __device__ __forceinline__ ff sphere_distance_ff(ff b, ff r2, ff cut2) {
-  return sphere_distance_ffc(b, ff_add(r2, ff_neg(cut2)));
+  return sphere_distance_ffc<SHORT>(b, ff_add(r2, ff_neg(cut2)));
 }
 
 __device__ __forceinline__ float bb_lookup(const float4* __restrict__ tab, float T, float t_min, float t_max,

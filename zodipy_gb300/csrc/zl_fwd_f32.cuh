@@ -127,6 +127,8 @@ __device__ __forceinline__ void pixel_setup_obs(const KParamsF32& P, const doubl
   using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
   const int nc = L::generic ? P.n_comps : NC;
   const int nr = P.n_ranges;
+  // the Planck layout's kernels keep the IEEE-division roots (measured faster there)
+  constexpr bool kShortRoots = LAYOUT != kLayoutPlanck;
   // float-float values of the doubles by bit operations (no float64 instruction); the sums
   // below are ff_add_fast (accurate to a few 2^-48 of their operands: the geometry needs
   // absolute, not relative, accuracy); only |X_obs|^2 - cutoff^2, per observer, is an exact sum
@@ -144,8 +146,8 @@ __device__ __forceinline__ void pixel_setup_obs(const KParamsF32& P, const doubl
 #pragma unroll
   for (int r = 0; r < ZL_MAX_RANGES; ++r) {
     if (r < nr) {
-      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_in[r]);
-      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc(b, Q.c_out[r]);
+      const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc<kShortRoots>(b, Q.c_in[r]);
+      const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f} : sphere_distance_ffc<kShortRoots>(b, Q.c_out[r]);
       hs_r[r] = ff_scale(ff_add_fast(sp, ff_neg(st)), 0.5f);
       mid_r[r] = ff_scale(ff_add_fast(sp, st), 0.5f);
     } else {
@@ -242,6 +244,8 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   using Fl = KFlags<LAYOUT == kLayoutGeneric ? kFlagsRuntime : FLAGS>;
   const int nc = L::generic ? P.n_comps : NC;
   const int nr = P.n_ranges;
+  // the Planck layout's kernels keep the IEEE-division roots (measured faster there)
+  constexpr bool kShortRoots = LAYOUT != kLayoutPlanck;
   // float-float values of the doubles by bit operations (no float64 instruction); the sums
   // below are ff_add_fast (accurate to a few 2^-48 of their operands: the geometry needs
   // absolute, not relative, accuracy); only |X_obs|^2 - cutoff^2, per observer, is an exact sum
@@ -262,9 +266,9 @@ __device__ __forceinline__ void pixel_setup(const KParamsF32& P, const double* _
   for (int r = 0; r < ZL_MAX_RANGES; ++r) {
     if (r < nr) {
       const ff st = ((outside >> (2 * r)) & 1u) ? ff{(float)kEps, 0.f}
-                                                : sphere_distance_ff(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
+                                                : sphere_distance_ff<kShortRoots>(b, r2, ff{P.cut_in_hi[r], P.cut_in_lo[r]});
       const ff sp = ((outside >> (2 * r + 1)) & 1u) ? ff{(float)kEps, 0.f}
-                                                    : sphere_distance_ff(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
+                                                    : sphere_distance_ff<kShortRoots>(b, r2, ff{P.cut_out_hi[r], P.cut_out_lo[r]});
       hs_r[r] = ff_scale(ff_add_fast(sp, ff_neg(st)), 0.5f);
       mid_r[r] = ff_scale(ff_add_fast(sp, st), 0.5f);
     } else {
