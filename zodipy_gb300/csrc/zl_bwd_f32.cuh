@@ -93,7 +93,8 @@ struct BwdPix {
   ff beta_h;                                     // obs . u
   float uxf, uyf, uzf, oxf, oyf, ozf, bperp;
   // squared impact parameters: |X|^2 = (R_los + obs . u)^2 + b2h about the Sun, and
-  // |X - X_0|^2 = (R_los + bc)^2 + b2c about an offset component's centre (bc = (obs - X_0) . u)
+  // |X - X_0|^2 = (R_los + bc)^2 + b2c about an offset component's centre (bc = (obs - X_0) . u;
+  // set with compiled flags only: with run-time flags comp_terms forms X - X_0 itself)
   float b2h;
   float bc[NC], b2c[NC];
   float un_c[NC], on_c[NC];                      // u . n_c and (obs - X_0,c) . n_c
