@@ -248,6 +248,7 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
   P->n_temps = m.n_temps;
   P->T0 = (float)m.T_0;
   P->neg_delta = (float)(-m.delta);
+  P->neg_half_delta = (float)(-0.5 * m.delta);
   P->t_min = (float)m.temps[0];
   P->t_max = (float)m.temps[m.n_temps - 1];
   P->inv_dt = (float)((m.n_temps - 1) / (m.temps[m.n_temps - 1] - m.temps[0]));
@@ -309,6 +310,7 @@ void build_f32(const ZlModel& m, KParamsF32* P) {
         K.c[4] = (float)p[3];
         K.c[5] = (float)(1.0 / (2.0 * p[3]));
         K.c[6] = (float)(p[3] / 2.0);
+        K.c[7] = (float)(-0.5 * p[0]);
         break;
       case ZL_BAND:
         K.c[0] = (float)(3.0 * C.n_0);

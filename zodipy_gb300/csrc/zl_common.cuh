@@ -57,7 +57,7 @@ struct KCompF32 {
   float ox, oy, oz;        // offset X_0 [AU]
   float ox_lo, oy_lo, oz_lo;  // low parts of X_0 for float-float geometry
   // type constants:
-  //  cloud:   c0=n_0, c1=alpha, c2=beta*log2(e), c3=gamma, c4=mu, c5=1/(2 mu), c6=mu/2
+  //  cloud:   c0=n_0, c1=alpha, c2=beta*log2(e), c3=gamma, c4=mu, c5=1/(2 mu), c6=mu/2, c7=-alpha/2
   //  band:    c0=3 n_0, c1=1/delta_zeta_rad, c2=1/v, c3=p, c4=1/delta_r^2, c5=(p==4)
   //  ring:    c0=n_0, c1=R, c2=log2(e)/sigma_r^2, c3=log2(e)/sigma_z, c4=R^2 (hi), c5=R^2 (lo)
   //  feature: c0=n_0, c1=R, c2=log2(e)/sigma_r^2, c3=log2(e)/sigma_z, c4=R^2 (hi), c5=R^2 (lo),
@@ -85,7 +85,7 @@ struct KSpecF32 {
 
 struct KParamsF32 {
   int32_t n_comps, n_ranges, n_spec, n_nodes, n_temps, has_scat;
-  float T0, neg_delta, t_min, t_max, inv_dt, pad0;
+  float T0, neg_delta, t_min, t_max, inv_dt, neg_half_delta;  // neg_half_delta = -delta / 2 (T from lg2 R^2)
   double cut_in[ZL_MAX_RANGES], cut_out[ZL_MAX_RANGES];
   float cut_in_hi[ZL_MAX_RANGES], cut_in_lo[ZL_MAX_RANGES];
   float cut_out_hi[ZL_MAX_RANGES], cut_out_lo[ZL_MAX_RANGES];

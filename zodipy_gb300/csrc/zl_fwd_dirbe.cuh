@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
       const float R2 = fmaf(wh, wh, PS.b2h);
       float rinv = rsqrt_ftz(R2);
       rinv = rinv * fmaf(-0.5f * R2, rinv * rinv, 1.5f);
-      const float T0 = P.T0 * ex2_ftz(P.neg_delta * lg2_ftz(R2 * rinv));  // blackbody.py:16-30
+      const float T0 = P.T0 * ex2_ftz(P.neg_half_delta * lg2_ftz(R2));  // R^-delta, blackbody.py:16-30
       float wB0[NSPEC], wS0[NSPEC];
 #pragma unroll
       for (int s = 0; s < NSPEC; ++s) {
@@ -161,12 +161,11 @@ __global__ void __launch_bounds__(128, (QUEUE && NSPEC == 1 && !((FLAGS >> 1) & 
         const float wc = lin_ff(PS.hs[0], xk, PS.wm[0]);
         const float Rc2 = fmaf(wc, wc, PS.b2[0]);
         const float rcinv = rsqrt_ftz(Rc2);
-        const float lg2Rc = 0.5f * lg2_ftz(Rc2);
         const float Z = lin_ff(PS.z1[0], xk, PS.z0[0]);
         const float zeta = fabsf(Z) * rcinv;
         const float g = zeta < Cc.c[4] ? zeta * zeta * Cc.c[5] : zeta - Cc.c[6];
         const float gg = ex2_ftz(Cc.c[3] * lg2_ftz(g));
-        const float dens = ex2_ftz(-Cc.c[1] * lg2Rc - Cc.c[2] * gg);
+        const float dens = ex2_ftz(Cc.c[7] * lg2_ftz(Rc2) - Cc.c[2] * gg);  // Rc^-alpha e^(-beta g^gamma)
 #pragma unroll
         for (int s = 0; s < NSPEC; ++s) {
           ps0[s] = fmaf(wB0[s], dens, ps0[s]);
